@@ -1,0 +1,288 @@
+/*
+ * rtg.h — C ABI of librtg, the GB300 (sm_103a) implementation of RT-Graph's
+ * sorted-adjacency set-intersection path: triangle counting (TC) and batched
+ * pairwise set-intersection counting (SI).
+ *
+ * Every entry point is plain C: pointers, sizes and status codes, no C++ or torch
+ * types. Every function returns an rtg_status and never calls exit(); the text of
+ * the last error on a context is available from rtg_last_error().
+ *
+ * Reference interfaces replaced (paths are relative to the RT-Graph repository):
+ *   - Graph::ReadBinaryEdges / TCPreprocessing / ConvertToCSR / Txt2Bin
+ *       tc/graph/include/graph.h:13-20, tc/graph/graph.cpp:23-214
+ *   - void CountOnGPU(int *adjs, int *offsets, int nodes, int edges, int device_id)
+ *       tc/bs_tc/bs_tc.h:5, tc/bs_tc/bs_tc.cu:232-354
+ *   - class RTTC { BuildBVHAndComputeRay; CountTriangles; total_triangles_ }
+ *       tc/rt_tc/include/rt_tc.h:7-59
+ *   - XxxBasedIntersection(const Dataset&, uint blocks, uint block_size, std::vector<uint>&)
+ *       set_intersection/baseline/bs.cu:21-22, hi.cu:22-23, ip.cu:32-33,
+ *       bi_naive.cu:26-27, bi_dynamic.cu:24-25
+ *   - class RTInter { BuildBVHAndComputeRay(Dataset); CountIntersection(std::vector<uint>&) }
+ *       set_intersection/rt/include/rt_intersection.h:7-29
+ *   - ReadData / Check / struct Dataset
+ *       set_intersection/utils/util.h:19-36, util.cpp:3-51
+ *
+ * Threading: one rtg_ctx per host thread; a context owns one CUDA stream and all
+ * calls on it are ordered on that stream. Graphs and set collections belong to the
+ * context that created them.
+ */
+#ifndef RTG_H
+#define RTG_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define RTG_ABI_VERSION 1
+
+/* Status codes. The reference prints and calls exit(2) on any CUDA error
+ * (tc/utils/common.h:13-32); librtg returns one of these instead. */
+typedef enum rtg_status {
+    RTG_OK = 0,
+    RTG_ERR_INVALID_ARG = 1, /* null pointer, size out of range, unsorted list ... */
+    RTG_ERR_OOM = 2,         /* device or pinned-host allocation failed            */
+    RTG_ERR_IO = 3,          /* file could not be opened / read / written          */
+    RTG_ERR_FORMAT = 4,      /* malformed input file                               */
+    RTG_ERR_DEVICE = 5,      /* CUDA runtime error (text in rtg_last_error)        */
+    RTG_ERR_TIMEOUT = 6,     /* a bounded device wait ran out (status word)        */
+    RTG_ERR_CANCELLED = 7,   /* request cancelled before completion                */
+    RTG_ERR_STATE = 8,       /* call out of order, e.g. count before rtg_csr_build */
+    RTG_ERR_BUSY = 9         /* admission refused: no slot or memory budget left   */
+} rtg_status;
+
+typedef struct rtg_ctx rtg_ctx;
+typedef struct rtg_graph rtg_graph;
+typedef struct rtg_sets rtg_sets;
+
+/* Input formats of rtg_graph_load.
+ *  EDGE_BIN : int32 (src,dst) pairs back to back, the reference's binary edge list
+ *             (tc/graph/graph.cpp:23-38).
+ *  EDGE_TXT : "src dst" per line, as read by Graph::Txt2Bin (graph.cpp:179-214).
+ *  MTX      : MatrixMarket coordinate file, 1-based (bfs/graph/graph.cpp:17-122). */
+typedef enum rtg_format { RTG_FMT_EDGE_BIN = 0, RTG_FMT_EDGE_TXT = 1, RTG_FMT_MTX = 2 } rtg_format;
+
+/* CSR kinds built by rtg_csr_build.
+ *  DEGREE          : simple undirected graph (self loops and duplicates removed), each
+ *                    edge oriented from the endpoint of lower degree to the higher one,
+ *                    ties to the smaller id. Vertex ids are kept.
+ *  DEGREE_RAW_REF  : the reference's exact preprocessing, bit for bit: ids compacted to
+ *                    dense ranks (graph.cpp:40-62), orientation by the degree counted on
+ *                    the raw list including duplicates (graph.cpp:108-124), vertices of
+ *                    raw degree <= 1 dropped and ids renumbered (graph.cpp:126-149),
+ *                    then sort, duplicate and self-loop removal, CSR (graph.cpp:154-173,
+ *                    71-102).
+ *  SYMMETRIC       : unoriented simple graph, both directions stored (used for vertex-
+ *                    pair queries). Held beside the oriented CSR, not in place of it. */
+typedef enum rtg_orient {
+    RTG_ORIENT_DEGREE = 0,
+    RTG_ORIENT_DEGREE_RAW_REF = 1,
+    RTG_ORIENT_SYMMETRIC = 2
+} rtg_orient;
+
+/* Triangle-count execution forms.
+ *  PLAIN   : one kernel launch per work bucket, one warp per oriented edge, host-driven,
+ *            fixed default schedule.
+ *  BATCHED : persistent kernel over a device work queue of (vertex, edge-range) items,
+ *            out-list of the source vertex staged in shared memory, launched as one
+ *            CUDA graph, schedule from the context configuration (autotuned). */
+typedef enum rtg_tc_mode { RTG_TC_PLAIN = 0, RTG_TC_BATCHED = 1 } rtg_tc_mode;
+
+/* Set-intersection kernel families (flags of rtg_si_count*). AUTO picks per pair by
+ * the length ratio. The forced families back the reference's per-baseline CLIs. */
+#define RTG_SI_AUTO 0u
+#define RTG_SI_FORCE_MERGE 1u   /* warp merge path (ip.cu)                        */
+#define RTG_SI_FORCE_SEARCH 2u  /* short list searched in the long list (bs.cu)   */
+#define RTG_SI_FORCE_BITMAP 3u  /* block bitmap / hash probe (bi_dynamic.cu, hi.cu) */
+#define RTG_SI_FAMILY_MASK 0xFu
+#define RTG_PAIRS_DEVICE 0x100u /* pair arrays are device pointers                 */
+#define RTG_OUT_DEVICE 0x200u   /* output array is a device pointer                */
+
+/* Per-call timing and counters. All times in milliseconds. Device times come from CUDA
+ * events on the context stream. */
+typedef struct rtg_timing {
+    double h2d_ms;            /* host -> device copies made by the call           */
+    double build_ms;          /* CSR build / set upload stage                     */
+    double count_ms;          /* counting stage (all kernels of the stage)        */
+    double main_kernel_ms;    /* the dominant counting kernel alone               */
+    double d2h_ms;            /* device -> host copies made by the call           */
+    double total_ms;          /* host wall time of the call                       */
+    uint64_t kernel_launches; /* librtg kernels launched by the call (graph nodes
+                                 count one each)                                   */
+    uint64_t algo_bytes;      /* algorithmic bytes of the counting stage          */
+    uint64_t h2d_bytes;
+    uint64_t d2h_bytes;
+} rtg_timing;
+
+typedef struct rtg_graph_info {
+    uint32_t n;              /* vertices of the oriented CSR                      */
+    uint64_t m_input;        /* input (raw) edges                                 */
+    uint64_t m;              /* edges of the oriented CSR = undirected simple m   */
+    uint32_t max_out_degree; /* max d+ of the oriented CSR                        */
+    uint64_t work_elems;     /* sum over oriented (u,v) of d+(u)+d+(v)            */
+    int32_t orient;          /* rtg_orient of the oriented CSR, -1 if not built   */
+    int32_t has_symmetric;   /* 1 when the symmetric CSR is built                 */
+    uint32_t n_sym;          /* vertices of the symmetric CSR                     */
+    uint64_t m_sym;          /* directed entries of the symmetric CSR (= 2 m)     */
+} rtg_graph_info;
+
+/* Tunable schedule of the BATCHED triangle count and of the SI pair kernels. Zero in
+ * any field means "library default". */
+typedef struct rtg_config {
+    uint32_t tc_block_warps;    /* warps per block of the persistent TC kernel        */
+    uint32_t tc_item_edges;     /* oriented edges per work item                       */
+    uint32_t tc_hash_slots;     /* shared-memory hash slots per warp (power of two)   */
+    uint32_t tc_blocks_per_sm;  /* resident blocks per SM of the persistent kernel    */
+    uint32_t si_block_warps;    /* warps per block of the SI kernels                  */
+    uint32_t si_search_ratio;   /* long/short length ratio above which SEARCH is used */
+    uint32_t si_split_len;      /* pairs with |A|+|B| above this are split by merge
+                                   path across warps                                  */
+    uint32_t si_pairs_per_grab; /* pairs a warp takes from the queue per fetch        */
+} rtg_config;
+
+/* ---------------------------------------------------------------- context */
+rtg_status rtg_init(int device, rtg_ctx **out);
+void rtg_destroy(rtg_ctx *ctx);
+const char *rtg_last_error(const rtg_ctx *ctx);
+const char *rtg_status_str(rtg_status s);
+int rtg_abi_version(void);
+rtg_status rtg_set_config(rtg_ctx *ctx, const rtg_config *cfg);
+rtg_status rtg_get_config(const rtg_ctx *ctx, rtg_config *cfg);
+/* Cumulative number of librtg kernel launches on this context. */
+uint64_t rtg_kernel_launches(const rtg_ctx *ctx);
+rtg_status rtg_synchronize(rtg_ctx *ctx);
+/* Overwrite a device buffer larger than L2 so the next call starts cold. */
+rtg_status rtg_flush_l2(rtg_ctx *ctx);
+/* Device properties used by schedules (SM count, shared memory per block). */
+rtg_status rtg_device_info(const rtg_ctx *ctx, int *sm_count, int *smem_per_block_optin,
+                           int *cc_major, int *cc_minor);
+/* Pinned host memory for callers that want page-locked staging buffers. */
+rtg_status rtg_host_alloc(rtg_ctx *ctx, size_t bytes, void **out);
+void rtg_host_free(void *p);
+
+/* ----------------------------------------------------------------- graphs */
+/* Edges as two uint32 arrays (host). The arrays are copied; the caller keeps them. */
+rtg_status rtg_graph_from_host_edges(rtg_ctx *ctx, const uint32_t *src, const uint32_t *dst,
+                                     uint64_t m, rtg_graph **out);
+/* Edges in the reference's edge_t layout: int32 {src,dst} pairs (tc/utils/model.h:16-29). */
+rtg_status rtg_graph_from_host_pairs(rtg_ctx *ctx, const int32_t *pairs, uint64_t m,
+                                     rtg_graph **out);
+/* Edges already on the device (copied into the graph). */
+rtg_status rtg_graph_from_device_edges(rtg_ctx *ctx, const uint32_t *d_src,
+                                       const uint32_t *d_dst, uint64_t m, rtg_graph **out);
+rtg_status rtg_graph_load(rtg_ctx *ctx, const char *path, rtg_format fmt, rtg_graph **out);
+/* Build a CSR on the GPU (radix sort, dedup, self-loop removal, orientation). */
+rtg_status rtg_csr_build(rtg_ctx *ctx, rtg_graph *g, rtg_orient orient);
+/* A CSR given directly by the caller (host arrays, int32 like the reference's
+ * Graph::adjs_/offsets_): rows must be sorted ascending and oriented (a DAG). */
+rtg_status rtg_graph_from_host_csr(rtg_ctx *ctx, const int32_t *offsets, const int32_t *adjs,
+                                   int32_t nodes, int64_t edges, rtg_graph **out);
+rtg_status rtg_graph_info_get(const rtg_graph *g, rtg_graph_info *info);
+/* Device pointers owned by the graph; valid until rtg_graph_destroy. */
+rtg_status rtg_csr_view(const rtg_graph *g, int symmetric, const uint64_t **d_offsets,
+                        const uint32_t **d_adj, uint32_t *n, uint64_t *m);
+/* Copy a CSR to caller-allocated host arrays (offsets: n+1 entries, adj: m entries). */
+rtg_status rtg_csr_to_host(rtg_ctx *ctx, const rtg_graph *g, int symmetric, uint64_t *offsets,
+                           uint32_t *adj);
+/* Free the raw edge buffer once the CSRs needed are built. */
+rtg_status rtg_graph_release_edges(rtg_graph *g);
+/* Device bytes currently held by the graph. */
+uint64_t rtg_graph_device_bytes(const rtg_graph *g);
+void rtg_graph_destroy(rtg_graph *g);
+
+/* ------------------------------------------------------ triangle counting */
+/* Exact uint64 triangle count of the oriented CSR of g. */
+rtg_status rtg_tc_count(rtg_ctx *ctx, rtg_graph *g, rtg_tc_mode mode, uint64_t *out_total,
+                        rtg_timing *timing);
+/* End to end from host edges: copy in, build the CSR with `orient`, count, copy the
+ * total out. The drop-in for the bs_tc / rt_tc pipelines. */
+rtg_status rtg_tc_count_host_edges(rtg_ctx *ctx, const uint32_t *src, const uint32_t *dst,
+                                   uint64_t m, rtg_orient orient, rtg_tc_mode mode,
+                                   uint64_t *out_total, rtg_timing *timing);
+/* Replaces CountOnGPU (tc/bs_tc/bs_tc.h:5): host int32 CSR in, count out (uint64
+ * instead of the reference's uint32). */
+rtg_status rtg_tc_count_host_csr(rtg_ctx *ctx, const int32_t *offsets, const int32_t *adjs,
+                                 int32_t nodes, int64_t edges, rtg_tc_mode mode,
+                                 uint64_t *out_total, rtg_timing *timing);
+/* |N(u) ∩ N(v)| on the symmetric CSR for each query pair (u[i], v[i]). */
+rtg_status rtg_graph_pair_count(rtg_ctx *ctx, rtg_graph *g, const uint32_t *u,
+                                const uint32_t *v, uint64_t npairs, uint32_t *out,
+                                uint32_t flags, rtg_timing *timing);
+
+/* --------------------------------------------------------- set collections */
+/* nsets sorted, duplicate-free uint32 lists; offsets has nsets+1 entries. */
+rtg_status rtg_sets_from_host(rtg_ctx *ctx, const uint64_t *offsets, uint64_t nsets,
+                              const uint32_t *elems, rtg_sets **out);
+/* The reference Dataset layout (uint32 offsets, set_intersection/utils/util.h:19-28). */
+rtg_status rtg_sets_from_host_u32(rtg_ctx *ctx, const uint32_t *offsets, uint32_t nsets,
+                                  const uint32_t *elems, rtg_sets **out);
+uint64_t rtg_sets_count(const rtg_sets *s);
+uint64_t rtg_sets_elems(const rtg_sets *s);
+void rtg_sets_destroy(rtg_sets *s);
+
+/* |S[pair_a[i]] ∩ S[pair_b[i]]| for i < npairs. flags: RTG_SI_* family, RTG_PAIRS_DEVICE,
+ * RTG_OUT_DEVICE. */
+rtg_status rtg_si_count(rtg_ctx *ctx, const rtg_sets *s, const uint32_t *pair_a,
+                        const uint32_t *pair_b, uint64_t npairs, uint32_t *out_counts,
+                        uint32_t flags, rtg_timing *timing);
+/* Dense |A| x |B| in the reference's row-major order (bs.cu:93-96,148):
+ * out[(a - a_begin) * (b_end - b_begin) + (b - b_begin)]. */
+rtg_status rtg_si_count_dense(rtg_ctx *ctx, const rtg_sets *s, uint32_t a_begin,
+                              uint32_t a_end, uint32_t b_begin, uint32_t b_end,
+                              uint32_t *out_counts, uint32_t flags, rtg_timing *timing);
+/* Materialised intersections: out_offsets (npairs+1 entries) and the elements of every
+ * intersection back to back in out_elems (capacity out_capacity entries; when it is too
+ * small the call fails with RTG_ERR_INVALID_ARG and out_offsets[npairs] holds the size
+ * needed). Host arrays. */
+rtg_status rtg_si_materialize(rtg_ctx *ctx, const rtg_sets *s, const uint32_t *pair_a,
+                              const uint32_t *pair_b, uint64_t npairs, uint64_t *out_offsets,
+                              uint32_t *out_elems, uint64_t out_capacity, rtg_timing *timing);
+
+/* --------------------------------------------------------- dataset files */
+/* Reference .s_data/.m_data header (set_intersection/utils/util.cpp:3-23 and
+ * data_generator/data.cpp:344-373). */
+typedef struct rtg_dataset_info {
+    uint32_t num_a;
+    uint32_t num_b;
+    uint32_t max_element;
+    uint32_t intersection;
+    uint64_t elems;
+} rtg_dataset_info;
+/* Two calls: with offsets/elems NULL it fills only `info`; then with arrays of
+ * num_a+num_b+1 and info.elems entries. */
+rtg_status rtg_dataset_read(const char *path, rtg_dataset_info *info, uint32_t *offsets,
+                            uint32_t *elems);
+rtg_status rtg_dataset_write(const char *path, const rtg_dataset_info *info,
+                             const uint32_t *offsets, const uint32_t *elems);
+/* Binary int32 edge list (the reference's .edge files). */
+rtg_status rtg_edges_write_bin(const char *path, const uint32_t *src, const uint32_t *dst,
+                               uint64_t m);
+/* Reads an edge file into host arrays; two calls as for rtg_dataset_read. */
+rtg_status rtg_edges_read(const char *path, rtg_format fmt, uint64_t *m, uint32_t *src,
+                          uint32_t *dst);
+
+/* ------------------------------------------------------ seeded generators */
+/* R-MAT: ef << scale edges, quadrant probabilities (a, b, c, 1-a-b-c). */
+rtg_status rtg_gen_rmat(uint32_t scale, uint32_t edge_factor, double a, double b, double c,
+                        uint64_t seed, uint32_t *src, uint32_t *dst);
+/* Barabasi-Albert: m*(n-m) + m edges (star seed on m+1 vertices). */
+rtg_status rtg_gen_ba(uint32_t n, uint32_t m, uint64_t seed, uint32_t *src, uint32_t *dst,
+                      uint64_t *m_out);
+/* Holme-Kim power-law cluster graph: m*(n-m) edges, triad closure probability p. */
+rtg_status rtg_gen_hk(uint32_t n, uint32_t m, double p, uint64_t seed, uint32_t *src,
+                      uint32_t *dst, uint64_t *m_out);
+/* Batched-SI pair workload. Phase 1 (elems == NULL): draws the list lengths into
+ * len (2*npairs entries) and the total into *total. Phase 2: fills offsets (2*npairs+1),
+ * elems (total) and expected[npairs] (the exact |A_i ∩ B_i| by construction). Pair i
+ * uses sets 2i and 2i+1. */
+rtg_status rtg_gen_si_pairs(uint64_t npairs, double median, double sigma, uint32_t min_len,
+                            uint32_t max_len, uint32_t universe_log2, double overlap_max,
+                            uint64_t seed, uint32_t *len, uint64_t *total, uint64_t *offsets,
+                            uint32_t *elems, uint32_t *expected);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* RTG_H */

@@ -1,0 +1,34 @@
+#!/usr/bin/env bash
+# Compile the reference's own host code for the TC preprocessing / two-hop counting and
+# the SI data generator, unmodified, from the sources where they lie under the reference
+# checkout, into oracle/_ref/ref_driver. TEST INFRASTRUCTURE ONLY: used to generate the
+# golden vectors under tests/golden/ that pin the oracle.
+#
+#   REF=/path/to/RT-Graph oracle/build_ref.sh
+#
+# Reference files used (read-only): tc/graph/graph.cpp, tc/bs_tc/bs_tc.cu (its host
+# function Preprocessing; the kernels in the same file compile but never run),
+# set_intersection/data_generator/data.cpp. ThrustSortEdgesInBatch is provided on the
+# host by oracle/ref_shim.cpp. CCCL 3 no longer pulls <vector>, <algorithm> and <cassert>
+# into bs_tc.cu, so they are force-included.
+set -euo pipefail
+REF="${REF:-/root/reference}"
+HERE="$(cd "$(dirname "$0")" && pwd)"
+OUT="$HERE/_ref"
+CUDA_HOME="${CUDA_HOME:-/usr/local/cuda}"
+if [ ! -d "$REF/tc/graph" ]; then
+  echo "reference sources not found at $REF" >&2
+  exit 2
+fi
+mkdir -p "$OUT"
+INC="-I$REF/tc/graph/include -I$REF/tc/utils -I$REF/tc/bs_tc -I$REF/set_intersection/data_generator -I$CUDA_HOME/include"
+g++ -O2 -fopenmp -std=c++17 $INC -c "$REF/tc/graph/graph.cpp" -o "$OUT/graph.o" &
+g++ -O2 -std=c++17 $INC -c "$REF/set_intersection/data_generator/data.cpp" -o "$OUT/data.o" &
+nvcc -O2 -std=c++17 -Xcompiler -fopenmp -include vector -include algorithm -include cassert \
+  $INC -gencode arch=compute_103a,code=sm_103a -c "$REF/tc/bs_tc/bs_tc.cu" -o "$OUT/bs_tc.o" &
+g++ -O2 -std=c++17 $INC -c "$HERE/ref_shim.cpp" -o "$OUT/ref_shim.o" &
+g++ -O2 -std=c++17 $INC -c "$HERE/ref_driver.cpp" -o "$OUT/ref_driver.o" &
+wait
+g++ -fopenmp -o "$OUT/ref_driver" "$OUT/ref_driver.o" "$OUT/ref_shim.o" "$OUT/graph.o" \
+  "$OUT/bs_tc.o" "$OUT/data.o" -L"$CUDA_HOME/lib64" -lcudart
+echo "built $OUT/ref_driver"

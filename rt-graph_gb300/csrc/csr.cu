@@ -1,0 +1,432 @@
+// GPU CSR builder.
+//
+// Edges are packed into 64-bit keys (hi << B | lo, B = bits needed for the largest id),
+// sorted with CUB's radix sort (only the 2B significant bits), deduplicated, and the CSR
+// offsets are written from the sorted keys without atomics.
+//
+// Two oriented forms are built:
+//  DEGREE          – simple graph first (self loops and duplicates removed on the
+//                    canonical (min,max) key), then each edge oriented from the lower
+//                    (degree, id) endpoint to the higher one.
+//  DEGREE_RAW_REF  – the reference preprocessing of tc/graph/graph.cpp, stage by stage:
+//                    ids compacted to dense ranks of the used ids (graph.cpp:40-62),
+//                    degree counted on the raw list including duplicates and self loops
+//                    (graph.cpp:108-114), orientation "swap when deg[src] > deg[dst] or
+//                    equal degrees and src > dst" (graph.cpp:116-124), vertices of raw
+//                    degree <= 1 dropped and ids shifted down by the number of dropped
+//                    smaller ids (graph.cpp:126-149), sort (graph.cpp:157), duplicates and
+//                    self loops removed (graph.cpp:160-173), CSR (graph.cpp:71-102).
+//  SYMMETRIC       – simple graph with both directions stored.
+#include <cub/cub.cuh>
+
+#include <algorithm>
+
+#include "internal.h"
+
+namespace rtg {
+
+namespace {
+
+constexpr int kThreads = 256;
+
+inline int grid_for(rtg_ctx *ctx, uint64_t n) {
+    uint64_t g = (n + kThreads - 1) / kThreads;
+    uint64_t cap = (uint64_t)ctx->sm_count * 16;
+    return (int)std::max<uint64_t>(1, std::min(g, cap));
+}
+
+inline int bits_for(uint64_t x) {  // bits needed to represent x (x >= 1)
+    int b = 0;
+    while (b < 64 && (x >> b)) ++b;
+    return std::max(b, 1);
+}
+
+#define GRID_STRIDE(i, n)                                                              \
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < (n);         \
+         i += (uint64_t)gridDim.x * blockDim.x)
+
+__global__ void k_max_id(const uint32_t *s, const uint32_t *d, uint64_t m, unsigned int *out) {
+    unsigned int mx = 0;
+    GRID_STRIDE(i, m) { mx = max(mx, max(s[i], d[i])); }
+    for (int o = 16; o; o >>= 1) mx = max(mx, __shfl_down_sync(0xffffffffu, mx, o));
+    if ((threadIdx.x & 31) == 0) atomicMax(out, mx);
+}
+
+// canonical undirected key; self loops become the sentinel
+__global__ void k_canon_keys(const uint32_t *s, const uint32_t *d, uint64_t m, int B,
+                             uint64_t sentinel, uint64_t *keys) {
+    GRID_STRIDE(i, m) {
+        uint32_t a = s[i], b = d[i];
+        keys[i] = (a == b) ? sentinel : (((uint64_t)min(a, b) << B) | max(a, b));
+    }
+}
+
+__global__ void k_degree_from_keys(const uint64_t *keys, uint64_t m, int B, uint32_t *deg) {
+    const uint64_t lo_mask = (1ull << B) - 1;
+    GRID_STRIDE(i, m) {
+        uint64_t k = keys[i];
+        atomicAdd(&deg[k >> B], 1u);
+        atomicAdd(&deg[k & lo_mask], 1u);
+    }
+}
+
+__global__ void k_orient_keys(uint64_t *keys, uint64_t m, int B, const uint32_t *deg) {
+    const uint64_t lo_mask = (1ull << B) - 1;
+    GRID_STRIDE(i, m) {
+        uint64_t k = keys[i];
+        uint32_t a = (uint32_t)(k >> B), b = (uint32_t)(k & lo_mask);  // a < b
+        uint32_t da = deg[a], db = deg[b];
+        bool keep = (da < db) || (da == db);  // ties go to the smaller id, which is a
+        keys[i] = keep ? k : (((uint64_t)b << B) | a);
+    }
+}
+
+__global__ void k_sym_keys(const uint64_t *ukeys, uint64_t m, int B, uint64_t *out) {
+    const uint64_t lo_mask = (1ull << B) - 1;
+    GRID_STRIDE(i, m) {
+        uint64_t k = ukeys[i];
+        uint64_t a = k >> B, b = k & lo_mask;
+        out[2 * i] = k;
+        out[2 * i + 1] = (b << B) | a;
+    }
+}
+
+// adj/src from sorted keys, offsets from the row boundaries
+__global__ void k_csr_fill(const uint64_t *keys, uint64_t m, int B, uint32_t n, uint32_t *adj,
+                           uint32_t *src, uint64_t *off) {
+    const uint64_t lo_mask = (1ull << B) - 1;
+    GRID_STRIDE(i, m) {
+        uint64_t k = keys[i];
+        uint32_t s = (uint32_t)(k >> B);
+        adj[i] = (uint32_t)(k & lo_mask);
+        if (src) src[i] = s;
+        int64_t prev = (i == 0) ? -1 : (int64_t)(keys[i - 1] >> B);
+        for (int64_t v = prev + 1; v <= (int64_t)s; ++v) off[v] = i;
+        if (i == m - 1)
+            for (uint64_t v = (uint64_t)s + 1; v <= n; ++v) off[v] = m;
+    }
+}
+
+__global__ void k_stats(const uint64_t *off, const uint32_t *adj, const uint32_t *src, uint64_t m,
+                        uint32_t n, unsigned long long *work, unsigned int *maxdeg) {
+    unsigned long long acc = 0;
+    unsigned int md = 0;
+    if (src) {
+        GRID_STRIDE(e, m) {
+            uint32_t u = src[e], v = adj[e];
+            acc += (off[u + 1] - off[u]) + (off[v + 1] - off[v]);
+        }
+    }
+    GRID_STRIDE(v, (uint64_t)n) { md = max(md, (unsigned int)(off[v + 1] - off[v])); }
+    for (int o = 16; o; o >>= 1) {
+        acc += __shfl_down_sync(0xffffffffu, acc, o);
+        md = max(md, __shfl_down_sync(0xffffffffu, md, o));
+    }
+    if ((threadIdx.x & 31) == 0) {
+        if (acc) atomicAdd(work, acc);
+        atomicMax(maxdeg, md);
+    }
+}
+
+// ---- reference-exact (DEGREE_RAW_REF) stages
+__global__ void k_mark_used(const uint32_t *s, const uint32_t *d, uint64_t m, uint32_t *used) {
+    GRID_STRIDE(i, m) {
+        used[s[i]] = 1u;
+        used[d[i]] = 1u;
+    }
+}
+
+__global__ void k_relabel_raw_degree(const uint32_t *s, const uint32_t *d, uint64_t m,
+                                     const uint32_t *rank, uint32_t *s2, uint32_t *d2,
+                                     uint32_t *deg) {
+    GRID_STRIDE(i, m) {
+        uint32_t a = rank[s[i]] - 1, b = rank[d[i]] - 1;
+        s2[i] = a;
+        d2[i] = b;
+        atomicAdd(&deg[a], 1u);
+        atomicAdd(&deg[b], 1u);
+    }
+}
+
+__global__ void k_flag_low_degree(const uint32_t *deg, uint32_t n, uint32_t *flag) {
+    GRID_STRIDE(v, (uint64_t)n) { flag[v] = deg[v] <= 1 ? 1u : 0u; }
+}
+
+__global__ void k_ref_orient_keys(const uint32_t *s2, const uint32_t *d2, uint64_t m,
+                                  const uint32_t *deg, const uint32_t *removes, int B,
+                                  uint64_t sentinel, uint64_t *keys) {
+    GRID_STRIDE(i, m) {
+        uint32_t a = s2[i], b = d2[i];
+        if (deg[a] > deg[b] || (deg[a] == deg[b] && a > b)) {
+            uint32_t t = a;
+            a = b;
+            b = t;
+        }
+        if (deg[a] <= 1 || deg[b] <= 1) {
+            keys[i] = sentinel;
+        } else {
+            a -= removes[a];
+            b -= removes[b];
+            keys[i] = ((uint64_t)a << B) | b;
+        }
+    }
+}
+
+__global__ void k_ref_keep_flags(const uint64_t *keys, uint64_t m, int B, uint64_t sentinel,
+                                 uint8_t *flags) {
+    const uint64_t lo_mask = (1ull << B) - 1;
+    GRID_STRIDE(i, m) {
+        uint64_t k = keys[i];
+        bool keep = k != sentinel && (k >> B) != (k & lo_mask) && (i == 0 || keys[i - 1] != k);
+        flags[i] = keep ? 1 : 0;
+    }
+}
+
+struct Buffers {
+    rtg_ctx *ctx;
+    std::vector<void *> owned;
+    ~Buffers() {
+        for (void *p : owned) dev_free(p);
+    }
+    template <class T>
+    rtg_status alloc(T **p, uint64_t count) {
+        void *q = nullptr;
+        RTG_TRY(dev_alloc(ctx, &q, count * sizeof(T)));
+        owned.push_back(q);
+        *p = (T *)q;
+        return RTG_OK;
+    }
+};
+
+rtg_status radix_sort(rtg_ctx *ctx, cub::DoubleBuffer<uint64_t> &db, uint64_t m, int end_bit) {
+    if (m < 2) return RTG_OK;
+    size_t bytes = 0;
+    RTG_CUDA(ctx, cub::DeviceRadixSort::SortKeys(nullptr, bytes, db, (int64_t)m, 0, end_bit,
+                                                 ctx->stream));
+    void *tmp = nullptr;
+    RTG_TRY(scratch(ctx, 0, bytes, &tmp));
+    RTG_CUDA(ctx, cub::DeviceRadixSort::SortKeys(tmp, bytes, db, (int64_t)m, 0, end_bit,
+                                                 ctx->stream));
+    ctx->launches += (end_bit + 7) / 8 + 1;
+    return RTG_OK;
+}
+
+template <class T>
+rtg_status inclusive_sum(rtg_ctx *ctx, const T *in, T *out, uint64_t n) {
+    size_t bytes = 0;
+    RTG_CUDA(ctx, cub::DeviceScan::InclusiveSum(nullptr, bytes, in, out, (int64_t)n, ctx->stream));
+    void *tmp = nullptr;
+    RTG_TRY(scratch(ctx, 0, bytes, &tmp));
+    RTG_CUDA(ctx, cub::DeviceScan::InclusiveSum(tmp, bytes, in, out, (int64_t)n, ctx->stream));
+    ctx->launches += 2;
+    return RTG_OK;
+}
+
+rtg_status read_u32(rtg_ctx *ctx, const uint32_t *d, uint32_t *h) {
+    RTG_CUDA(ctx, cudaMemcpyAsync(h, d, 4, cudaMemcpyDeviceToHost, ctx->stream));
+    RTG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    return RTG_OK;
+}
+
+// Fill a CSR (offsets, adj, optional src) from sorted keys and compute its stats.
+rtg_status fill_csr(rtg_ctx *ctx, const uint64_t *keys, uint64_t m, int B, uint32_t n,
+                    bool with_src, Csr &c) {
+    graph_free_csr(c);
+    c.n = n;
+    c.m = m;
+    RTG_TRY(dev_alloc(ctx, (void **)&c.off, (n + 1ull) * 8));
+    RTG_TRY(dev_alloc(ctx, (void **)&c.adj, m * 4));
+    if (with_src) RTG_TRY(dev_alloc(ctx, (void **)&c.src, m * 4));
+    if (m == 0) {
+        RTG_CUDA(ctx, cudaMemsetAsync(c.off, 0, (n + 1ull) * 8, ctx->stream));
+    } else {
+        k_csr_fill<<<grid_for(ctx, m), kThreads, 0, ctx->stream>>>(keys, m, B, n, c.adj, c.src,
+                                                                    c.off);
+        ctx->launches++;
+        RTG_CUDA(ctx, cudaGetLastError());
+    }
+    unsigned long long *w = ctx->d_scalars;
+    RTG_CUDA(ctx, cudaMemsetAsync(w, 0, 16, ctx->stream));
+    k_stats<<<grid_for(ctx, m + n), kThreads, 0, ctx->stream>>>(c.off, c.adj, c.src, m, n, w,
+                                                                 (unsigned int *)(w + 1));
+    ctx->launches++;
+    RTG_CUDA(ctx, cudaGetLastError());
+    unsigned long long h[2];
+    RTG_CUDA(ctx, cudaMemcpyAsync(h, w, 16, cudaMemcpyDeviceToHost, ctx->stream));
+    RTG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    c.work_elems = h[0];
+    c.max_deg = (uint32_t)h[1];
+    c.built = true;
+    return RTG_OK;
+}
+
+// Simple undirected edge keys (sorted, unique, no self loops). Returns the count in *mu.
+rtg_status simple_keys(rtg_ctx *ctx, rtg_graph *g, uint32_t maxid, int B, uint64_t *k0,
+                       uint64_t *k1, uint64_t **ukeys, uint64_t *mu) {
+    uint64_t m = g->m_input;
+    uint64_t sentinel = (uint64_t)(maxid + 1ull) << B;
+    int end_bit = std::min(64, B + bits_for(maxid + 1ull));
+    k_canon_keys<<<grid_for(ctx, m), kThreads, 0, ctx->stream>>>(g->d_src, g->d_dst, m, B,
+                                                                  sentinel, k0);
+    ctx->launches++;
+    RTG_CUDA(ctx, cudaGetLastError());
+    cub::DoubleBuffer<uint64_t> db(k0, k1);
+    RTG_TRY(radix_sort(ctx, db, m, end_bit));
+    uint64_t *sorted = db.Current();
+    uint64_t *uniq = db.Alternate();
+    int64_t *d_num = (int64_t *)(ctx->d_scalars + 4);
+    size_t bytes = 0;
+    RTG_CUDA(ctx, cub::DeviceSelect::Unique(nullptr, bytes, sorted, uniq, d_num, (int64_t)m,
+                                            ctx->stream));
+    void *tmp = nullptr;
+    RTG_TRY(scratch(ctx, 0, bytes, &tmp));
+    RTG_CUDA(ctx, cub::DeviceSelect::Unique(tmp, bytes, sorted, uniq, d_num, (int64_t)m,
+                                            ctx->stream));
+    ctx->launches += 2;
+    int64_t nu = 0;
+    RTG_CUDA(ctx, cudaMemcpyAsync(&nu, d_num, 8, cudaMemcpyDeviceToHost, ctx->stream));
+    RTG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    if (nu > 0) {
+        uint64_t last = 0;
+        RTG_CUDA(ctx, cudaMemcpyAsync(&last, uniq + nu - 1, 8, cudaMemcpyDeviceToHost,
+                                      ctx->stream));
+        RTG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+        if (last == sentinel) --nu;
+    }
+    *ukeys = uniq;
+    *mu = (uint64_t)nu;
+    return RTG_OK;
+}
+
+}  // namespace
+
+rtg_status build_csr(rtg_ctx *ctx, rtg_graph *g, rtg_orient orient) {
+    uint64_t m = g->m_input;
+    Buffers buf{ctx, {}};
+    // largest id
+    uint32_t maxid = 0;
+    if (m) {
+        unsigned int *d_mx = (unsigned int *)ctx->d_scalars;
+        RTG_CUDA(ctx, cudaMemsetAsync(d_mx, 0, 4, ctx->stream));
+        k_max_id<<<grid_for(ctx, m), kThreads, 0, ctx->stream>>>(g->d_src, g->d_dst, m, d_mx);
+        ctx->launches++;
+        RTG_CUDA(ctx, cudaGetLastError());
+        RTG_TRY(read_u32(ctx, d_mx, &maxid));
+        if (maxid == kEmpty)
+            return fail(ctx, RTG_ERR_INVALID_ARG, "vertex id 0xFFFFFFFF is reserved");
+    }
+
+    if (orient == RTG_ORIENT_DEGREE_RAW_REF) {
+        if (maxid > 0x7FFFFFFEu)
+            return fail(ctx, RTG_ERR_INVALID_ARG, "ids must fit int32 in reference mode");
+        if (m == 0) {
+            RTG_TRY(fill_csr(ctx, nullptr, 0, 1, 0, true, g->ori));
+            g->orient = orient;
+            return RTG_OK;
+        }
+        uint32_t *used, *rank, *s2, *d2, *deg, *removes;
+        RTG_TRY(buf.alloc(&used, maxid + 1ull));
+        RTG_TRY(buf.alloc(&rank, maxid + 1ull));
+        RTG_CUDA(ctx, cudaMemsetAsync(used, 0, (maxid + 1ull) * 4, ctx->stream));
+        k_mark_used<<<grid_for(ctx, m), kThreads, 0, ctx->stream>>>(g->d_src, g->d_dst, m, used);
+        ctx->launches++;
+        RTG_CUDA(ctx, cudaGetLastError());
+        RTG_TRY(inclusive_sum(ctx, used, rank, maxid + 1ull));
+        uint32_t n_used = 0;
+        RTG_TRY(read_u32(ctx, rank + maxid, &n_used));
+        RTG_TRY(buf.alloc(&s2, m));
+        RTG_TRY(buf.alloc(&d2, m));
+        RTG_TRY(buf.alloc(&deg, n_used));
+        RTG_TRY(buf.alloc(&removes, n_used));
+        RTG_CUDA(ctx, cudaMemsetAsync(deg, 0, n_used * 4ull, ctx->stream));
+        k_relabel_raw_degree<<<grid_for(ctx, m), kThreads, 0, ctx->stream>>>(
+            g->d_src, g->d_dst, m, rank, s2, d2, deg);
+        ctx->launches++;
+        k_flag_low_degree<<<grid_for(ctx, n_used), kThreads, 0, ctx->stream>>>(deg, n_used, used);
+        ctx->launches++;
+        RTG_CUDA(ctx, cudaGetLastError());
+        RTG_TRY(inclusive_sum(ctx, used, removes, (uint64_t)n_used));
+        uint32_t removed = 0;
+        RTG_TRY(read_u32(ctx, removes + n_used - 1, &removed));
+        uint32_t n_ref = n_used - removed;
+        int B = bits_for(std::max<uint64_t>(n_ref, 1));
+        uint64_t sentinel = (uint64_t)(n_ref + 1ull) << B;
+        // n_ref may be 0; sentinel hi = n_ref + 1 must still exceed every kept id
+        int end_bit = std::min(64, B + bits_for(n_ref + 1ull));
+        uint64_t *k0, *k1;
+        RTG_TRY(buf.alloc(&k0, m));
+        RTG_TRY(buf.alloc(&k1, m));
+        k_ref_orient_keys<<<grid_for(ctx, m), kThreads, 0, ctx->stream>>>(s2, d2, m, deg, removes,
+                                                                           B, sentinel, k0);
+        ctx->launches++;
+        RTG_CUDA(ctx, cudaGetLastError());
+        cub::DoubleBuffer<uint64_t> db(k0, k1);
+        RTG_TRY(radix_sort(ctx, db, m, end_bit));
+        uint8_t *flags;
+        RTG_TRY(buf.alloc(&flags, m));
+        k_ref_keep_flags<<<grid_for(ctx, m), kThreads, 0, ctx->stream>>>(db.Current(), m, B,
+                                                                          sentinel, flags);
+        ctx->launches++;
+        RTG_CUDA(ctx, cudaGetLastError());
+        int64_t *d_num = (int64_t *)(ctx->d_scalars + 4);
+        size_t bytes = 0;
+        RTG_CUDA(ctx, cub::DeviceSelect::Flagged(nullptr, bytes, db.Current(), flags,
+                                                 db.Alternate(), d_num, (int64_t)m, ctx->stream));
+        void *tmp = nullptr;
+        RTG_TRY(scratch(ctx, 0, bytes, &tmp));
+        RTG_CUDA(ctx, cub::DeviceSelect::Flagged(tmp, bytes, db.Current(), flags, db.Alternate(),
+                                                 d_num, (int64_t)m, ctx->stream));
+        ctx->launches += 2;
+        int64_t mk = 0;
+        RTG_CUDA(ctx, cudaMemcpyAsync(&mk, d_num, 8, cudaMemcpyDeviceToHost, ctx->stream));
+        RTG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+        RTG_TRY(fill_csr(ctx, db.Alternate(), (uint64_t)mk, B, n_ref, true, g->ori));
+        g->orient = orient;
+        return RTG_OK;
+    }
+
+    int B = bits_for(maxid + 1ull);
+    uint32_t n = m ? maxid + 1 : 0;
+    uint64_t *k0 = nullptr, *k1 = nullptr;
+    uint64_t cap = std::max<uint64_t>(m, 1);
+    if (orient == RTG_ORIENT_SYMMETRIC) cap = std::max<uint64_t>(2 * m, 1);
+    RTG_TRY(buf.alloc(&k0, cap));
+    RTG_TRY(buf.alloc(&k1, cap));
+    uint64_t *ukeys = k0;
+    uint64_t mu = 0;
+    if (m) RTG_TRY(simple_keys(ctx, g, maxid, B, k0, k1, &ukeys, &mu));
+    int end_bit = std::min(64, B + bits_for(maxid + 1ull));
+
+    if (orient == RTG_ORIENT_SYMMETRIC) {
+        uint64_t *other = (ukeys == k0) ? k1 : k0;
+        if (mu) {
+            k_sym_keys<<<grid_for(ctx, mu), kThreads, 0, ctx->stream>>>(ukeys, mu, B, other);
+            ctx->launches++;
+            RTG_CUDA(ctx, cudaGetLastError());
+        }
+        cub::DoubleBuffer<uint64_t> db(other, ukeys);
+        RTG_TRY(radix_sort(ctx, db, 2 * mu, end_bit));
+        RTG_TRY(fill_csr(ctx, db.Current(), 2 * mu, B, n, false, g->sym));
+        return RTG_OK;
+    }
+
+    // DEGREE
+    uint32_t *deg = nullptr;
+    RTG_TRY(buf.alloc(&deg, std::max<uint64_t>(n, 1)));
+    if (n) RTG_CUDA(ctx, cudaMemsetAsync(deg, 0, n * 4ull, ctx->stream));
+    if (mu) {
+        k_degree_from_keys<<<grid_for(ctx, mu), kThreads, 0, ctx->stream>>>(ukeys, mu, B, deg);
+        ctx->launches++;
+        k_orient_keys<<<grid_for(ctx, mu), kThreads, 0, ctx->stream>>>(ukeys, mu, B, deg);
+        ctx->launches++;
+        RTG_CUDA(ctx, cudaGetLastError());
+    }
+    uint64_t *other = (ukeys == k0) ? k1 : k0;
+    cub::DoubleBuffer<uint64_t> db(ukeys, other);
+    RTG_TRY(radix_sort(ctx, db, mu, end_bit));
+    RTG_TRY(fill_csr(ctx, db.Current(), mu, B, n, true, g->ori));
+    g->orient = orient;
+    return RTG_OK;
+}
+
+}  // namespace rtg

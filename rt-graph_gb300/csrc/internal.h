@@ -1,0 +1,139 @@
+// Internal declarations shared by the librtg translation units.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <cstdio>
+#include <string>
+#include <vector>
+
+#include "rtg.h"
+
+namespace rtg {
+
+// Sentinel used for empty hash slots and padding; vertex ids and set elements must be
+// smaller (checked on input).
+constexpr uint32_t kEmpty = 0xFFFFFFFFu;
+
+// Device status word values written by kernels (never a trap).
+constexpr uint32_t kStatusOk = 0;
+constexpr uint32_t kStatusTimeout = 1;
+constexpr uint32_t kStatusBadInput = 2;
+
+struct DeviceBuffer {
+    void *ptr = nullptr;
+    size_t bytes = 0;
+};
+
+// One oriented or symmetric CSR resident in HBM.
+struct Csr {
+    uint64_t *off = nullptr;  // n+1
+    uint32_t *adj = nullptr;  // m
+    uint32_t *src = nullptr;  // m, source vertex of each entry (oriented CSR only)
+    uint32_t n = 0;
+    uint64_t m = 0;
+    uint32_t max_deg = 0;
+    uint64_t work_elems = 0;  // sum over entries (u,v) of deg(u)+deg(v)
+    bool built = false;
+};
+
+struct TcPlan;   // cached per-graph counting plans (tc.cu)
+
+}  // namespace rtg
+
+struct rtg_ctx {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    std::string last_error;
+    rtg_config cfg{};
+    uint64_t launches = 0;
+    int sm_count = 0;
+    int smem_optin = 0;
+    int cc_major = 0, cc_minor = 0;
+    void *flush_buf = nullptr;
+    size_t flush_bytes = 0;
+    uint32_t *d_status = nullptr;        // device status word (kernels write errors here)
+    unsigned long long *d_scalars = nullptr;  // small device scratch for counters (16 words)
+    cudaEvent_t ev[8] = {};
+    // grow-only scratch for CUB temp storage and per-call buffers
+    rtg::DeviceBuffer scratch[6];
+};
+
+struct rtg_graph {
+    rtg_ctx *ctx = nullptr;
+    uint32_t *d_src = nullptr;  // raw edges on the device
+    uint32_t *d_dst = nullptr;
+    uint64_t m_input = 0;
+    bool edges_released = false;
+    rtg::Csr ori;               // oriented CSR
+    int orient = -1;
+    rtg::Csr sym;               // symmetric CSR
+    rtg::TcPlan *plan_batched = nullptr;
+    rtg::TcPlan *plan_plain = nullptr;
+};
+
+struct rtg_sets {
+    rtg_ctx *ctx = nullptr;
+    uint64_t *off = nullptr;  // nsets+1
+    uint32_t *elems = nullptr;
+    uint64_t nsets = 0;
+    uint64_t nelems = 0;
+    uint32_t max_len = 0;
+    bool borrowed = false;    // views a graph CSR (not freed here)
+};
+
+namespace rtg {
+
+// Error helpers: record the message on the context and return a status.
+rtg_status fail(rtg_ctx *ctx, rtg_status s, const char *fmt, ...);
+rtg_status cuda_fail(rtg_ctx *ctx, cudaError_t e, const char *what, const char *file, int line);
+
+#define RTG_CUDA(ctx, call)                                                        \
+    do {                                                                           \
+        cudaError_t e_ = (call);                                                   \
+        if (e_ != cudaSuccess) return ::rtg::cuda_fail((ctx), e_, #call, __FILE__, __LINE__); \
+    } while (0)
+
+#define RTG_TRY(expr)                       \
+    do {                                    \
+        rtg_status s_ = (expr);             \
+        if (s_ != RTG_OK) return s_;        \
+    } while (0)
+
+rtg_status dev_alloc(rtg_ctx *ctx, void **p, size_t bytes);
+void dev_free(void *p);
+// Grow-only scratch slot i of the context (contents undefined).
+rtg_status scratch(rtg_ctx *ctx, int slot, size_t bytes, void **p);
+rtg_status check_status_word(rtg_ctx *ctx);
+
+// CSR builder (csr.cu)
+rtg_status build_csr(rtg_ctx *ctx, rtg_graph *g, rtg_orient orient);
+rtg_status graph_free_csr(Csr &c);
+
+// Triangle counting (tc.cu)
+rtg_status tc_count(rtg_ctx *ctx, rtg_graph *g, rtg_tc_mode mode, uint64_t *total,
+                    rtg_timing *t);
+void tc_plan_free(TcPlan *p);
+
+// Set intersection (si.cu). Sets are any CSR-like (off, elems); pairs may be implicit
+// dense A x B (dense_nb > 0: pair k = (a_begin + k / dense_nb, b_begin + k % dense_nb)).
+struct PairSpec {
+    const uint64_t *off = nullptr;
+    const uint32_t *elems = nullptr;
+    uint64_t nsets = 0;
+    const uint32_t *pa = nullptr;  // device
+    const uint32_t *pb = nullptr;  // device
+    uint64_t npairs = 0;
+    uint32_t dense_nb = 0;
+    uint32_t a_begin = 0, b_begin = 0;
+};
+rtg_status si_count_device(rtg_ctx *ctx, const PairSpec &ps, uint32_t *d_out, uint32_t family,
+                           float *kernel_ms, uint64_t *launches);
+rtg_status si_materialize_device(rtg_ctx *ctx, const PairSpec &ps, uint64_t *d_out_off,
+                                 uint32_t *d_out_elems, uint64_t capacity, uint64_t *needed,
+                                 uint64_t *launches);
+
+double now_ms();
+
+}  // namespace rtg

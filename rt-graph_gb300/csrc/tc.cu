@@ -1,0 +1,446 @@
+// Triangle counting on the oriented CSR.
+//
+// Every triangle {u, v, w} of the simple graph appears exactly once as an oriented edge
+// u->v with w in N+(u) ∩ N+(v); the count is the sum over oriented edges of
+// |N+(u) ∩ N+(v)| (the reference computes the same sum edge by edge with binary searches,
+// tc/bs_tc/bs_tc.cu:120-148, or from aggregated two-hop triples, bs_tc.cu:153-229).
+//
+// PLAIN   : classify edges into (family, size) buckets, copy the bucket sizes to the host,
+//           scatter edge ids per bucket, then one grid-stride launch per bucket with one warp
+//           per edge (merge family for balanced pairs, search family for skewed ones).
+// BATCHED : work items (u, first edge) of up to E out-edges of one source vertex, built on
+//           the device; one persistent kernel whose warps take items from an atomic queue,
+//           hash N+(u) once into the warp's shared-memory table and stream every N+(v)
+//           through it. The item build and the count are captured once in a CUDA graph and
+//           replayed. uint64 totals: lane partials -> warp shuffle sum -> block sum -> one
+//           atomicAdd per block.
+#include <cub/cub.cuh>
+
+#include <algorithm>
+
+#include "internal.h"
+#include "intersect.cuh"
+
+namespace rtg {
+
+namespace {
+
+constexpr uint32_t kDefaultItemEdges = 64;
+constexpr uint32_t kDefaultHashSlots = 2048;
+constexpr uint32_t kDefaultBlockWarps = 8;
+constexpr uint32_t kPlainRatio = 16;    // long/short above this -> search family (PLAIN)
+constexpr int kPlainBuckets = 6;         // 2 families x 3 size classes
+
+__device__ __forceinline__ void block_add_total(unsigned long long v, unsigned long long *total,
+                                                unsigned long long *red) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    v = warp_sum_u64(v);
+    if (lane == 0) red[warp] = v;
+    __syncthreads();
+    if (warp == 0) {
+        unsigned long long s = (lane < nw) ? red[lane] : 0ull;
+        s = warp_sum_u64(s);
+        if (lane == 0 && s) atomicAdd(total, s);
+    }
+}
+
+// ------------------------------------------------------------------ PLAIN form
+
+__global__ void k_plain_classify(const uint64_t *__restrict__ off, const uint32_t *__restrict__ adj,
+                                 const uint32_t *__restrict__ src, uint64_t m, uint8_t *bucket,
+                                 unsigned long long *counts) {
+    __shared__ unsigned int local[kPlainBuckets];
+    if (threadIdx.x < kPlainBuckets) local[threadIdx.x] = 0;
+    __syncthreads();
+    for (uint64_t e = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; e < m;
+         e += (uint64_t)gridDim.x * blockDim.x) {
+        uint32_t u = src[e], v = adj[e];
+        uint32_t a = (uint32_t)(off[u + 1] - off[u]), b = (uint32_t)(off[v + 1] - off[v]);
+        uint8_t id = 0xFF;
+        if (a >= 2 && b >= 1) {
+            uint32_t lo = min(a, b), hi = max(a, b);
+            uint32_t fam = (hi > kPlainRatio * lo) ? 1u : 0u;
+            uint32_t sum = a + b;
+            uint32_t cls = sum <= 128 ? 0u : (sum <= 1024 ? 1u : 2u);
+            id = (uint8_t)(fam * 3 + cls);
+            atomicAdd(&local[id], 1u);
+        }
+        bucket[e] = id;
+    }
+    __syncthreads();
+    if (threadIdx.x < kPlainBuckets && local[threadIdx.x])
+        atomicAdd(&counts[threadIdx.x], (unsigned long long)local[threadIdx.x]);
+}
+
+__global__ void k_plain_scatter(const uint8_t *__restrict__ bucket, uint64_t m,
+                                const unsigned long long *__restrict__ base,
+                                unsigned long long *cursor, uint32_t *lists) {
+    for (uint64_t e = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; e < m;
+         e += (uint64_t)gridDim.x * blockDim.x) {
+        uint8_t id = bucket[e];
+        if (id == 0xFF) continue;
+        unsigned long long p = atomicAdd(&cursor[id], 1ull);
+        lists[base[id] + p] = (uint32_t)e;
+    }
+}
+
+template <bool kSearch>
+__global__ void __launch_bounds__(256) k_plain_edges(const uint64_t *__restrict__ off,
+                                                    const uint32_t *__restrict__ adj,
+                                                    const uint32_t *__restrict__ src,
+                                                    const uint32_t *__restrict__ list, uint64_t ne,
+                                                    unsigned long long *total) {
+    __shared__ unsigned long long red[8];
+    const int lane = threadIdx.x & 31;
+    uint64_t warp = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5;
+    uint64_t nwarps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
+    unsigned long long cnt = 0;
+    for (uint64_t k = warp; k < ne; k += nwarps) {
+        uint32_t e = list[k];
+        uint32_t u = src[e], v = adj[e];
+        uint64_t ou = off[u], ov = off[v];
+        uint32_t a = (uint32_t)(off[u + 1] - ou), b = (uint32_t)(off[v + 1] - ov);
+        const uint32_t *A = adj + ou, *B = adj + ov;
+        if (kSearch) {
+            if (a <= b) cnt += warp_search_count(A, a, B, b, lane);
+            else cnt += warp_search_count(B, b, A, a, lane);
+        } else {
+            cnt += warp_merge_count(A, a, B, b, lane);
+        }
+    }
+    block_add_total(cnt, total, red);
+}
+
+// ---------------------------------------------------------------- BATCHED form
+
+__global__ void k_item_counts(const uint64_t *__restrict__ off, uint32_t n, uint32_t E,
+                              uint32_t *cnt) {
+    for (uint64_t u = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; u <= n;
+         u += (uint64_t)gridDim.x * blockDim.x) {
+        uint32_t c = 0;
+        if (u < n) {
+            uint32_t a = (uint32_t)(off[u + 1] - off[u]);
+            c = (a >= 2) ? (a + E - 1) / E : 0u;
+        }
+        cnt[u] = c;
+    }
+}
+
+__global__ void k_item_fill(const uint64_t *__restrict__ off, uint32_t n, uint32_t E,
+                            const uint32_t *__restrict__ base, uint64_t *items,
+                            unsigned long long *acc) {
+    for (uint64_t u = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; u < n;
+         u += (uint64_t)gridDim.x * blockDim.x) {
+        uint32_t a = (uint32_t)(off[u + 1] - off[u]);
+        if (a < 2) continue;
+        uint32_t b0 = base[u];
+        uint32_t k = 0;
+        for (uint32_t j = 0; j < a; j += E, ++k) items[b0 + k] = (u << 32) | j;
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) acc[2] = base[n];
+}
+
+// acc[0] = total, acc[1] = queue head, acc[2] = number of items
+__global__ void k_tc_batched(const uint64_t *__restrict__ off, const uint32_t *__restrict__ adj,
+                             const uint64_t *__restrict__ items, unsigned long long *acc,
+                             uint32_t E, uint32_t H) {
+    extern __shared__ __align__(16) uint32_t smem[];
+    __shared__ unsigned long long red[32];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    uint32_t *tab = smem + warp * H;
+    const unsigned long long nitems = acc[2];
+    unsigned long long cnt = 0;
+    while (true) {
+        unsigned long long k = 0;
+        if (lane == 0) k = atomicAdd(&acc[1], 1ull);
+        k = __shfl_sync(kFull, k, 0);
+        if (k >= nitems) break;
+        const uint64_t it = items[k];
+        const uint32_t u = (uint32_t)(it >> 32), j0 = (uint32_t)it;
+        const uint64_t ou = off[u];
+        const uint32_t a = (uint32_t)(off[u + 1] - ou);
+        const uint32_t j1 = min(j0 + E, a);
+        const uint32_t *Nu = adj + ou;
+        const bool hashed = a <= H / 2;
+        uint32_t lg = 0;
+        if (hashed) {
+            lg = hash_lg_for(a);
+            warp_hash_build(tab, lg, Nu, a, lane);
+        }
+        for (uint32_t jb = j0; jb < j1; jb += 32) {
+            // the next (up to) 32 out-neighbours v and their list bounds, one per lane
+            const uint32_t j = jb + lane;
+            const bool ok = j < j1;
+            const uint32_t v = ok ? __ldg(Nu + j) : 0u;
+            const uint64_t ov = ok ? __ldg(off + v) : 0ull;
+            const uint32_t bl = ok ? (uint32_t)(__ldg(off + v + 1) - ov) : 0u;
+            const uint32_t ne = min(32u, j1 - jb);
+            for (uint32_t e = 0; e < ne; ++e) {
+                const uint64_t ove = __shfl_sync(kFull, ov, e);
+                const uint32_t be = __shfl_sync(kFull, bl, e);
+                if (be == 0) continue;
+                const uint32_t *Nv = adj + ove;
+                if (hashed) cnt += warp_hash_stream(tab, lg, Nv, be, lane);
+                else cnt += warp_merge_count(Nu, a, Nv, be, lane);
+            }
+        }
+        __syncwarp();
+    }
+    block_add_total(cnt, &acc[0], red);
+}
+
+}  // namespace
+
+struct TcPlan {
+    rtg_tc_mode mode = RTG_TC_BATCHED;
+    rtg_config cfg{};
+    // batched
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    uint64_t *items = nullptr;
+    uint32_t *vcnt = nullptr;
+    void *cub_tmp = nullptr;
+    unsigned long long *acc = nullptr;
+    cudaEvent_t k0 = nullptr, k1 = nullptr;
+    uint64_t graph_kernels = 0;
+    // plain
+    uint8_t *bucket = nullptr;
+    uint32_t *lists = nullptr;
+    cudaEvent_t bev[2 * kPlainBuckets] = {};
+};
+
+void tc_plan_free(TcPlan *p) {
+    if (!p) return;
+    if (p->exec) cudaGraphExecDestroy(p->exec);
+    if (p->graph) cudaGraphDestroy(p->graph);
+    dev_free(p->items);
+    dev_free(p->vcnt);
+    dev_free(p->cub_tmp);
+    dev_free(p->acc);
+    dev_free(p->bucket);
+    dev_free(p->lists);
+    if (p->k0) cudaEventDestroy(p->k0);
+    if (p->k1) cudaEventDestroy(p->k1);
+    for (auto ev : p->bev)
+        if (ev) cudaEventDestroy(ev);
+    delete p;
+}
+
+namespace {
+
+rtg_config effective_config(const rtg_ctx *ctx) {
+    rtg_config c = ctx->cfg;
+    if (!c.tc_item_edges) c.tc_item_edges = kDefaultItemEdges;
+    if (!c.tc_hash_slots) c.tc_hash_slots = kDefaultHashSlots;
+    if (!c.tc_block_warps) c.tc_block_warps = kDefaultBlockWarps;
+    return c;
+}
+
+bool same_tc_config(const rtg_config &a, const rtg_config &b) {
+    return a.tc_item_edges == b.tc_item_edges && a.tc_hash_slots == b.tc_hash_slots &&
+           a.tc_block_warps == b.tc_block_warps && a.tc_blocks_per_sm == b.tc_blocks_per_sm;
+}
+
+rtg_status batched_plan(rtg_ctx *ctx, rtg_graph *g, TcPlan **out) {
+    rtg_config cfg = effective_config(ctx);
+    if (g->plan_batched && same_tc_config(g->plan_batched->cfg, cfg)) {
+        *out = g->plan_batched;
+        return RTG_OK;
+    }
+    tc_plan_free(g->plan_batched);
+    g->plan_batched = nullptr;
+    TcPlan *p = new TcPlan();
+    p->mode = RTG_TC_BATCHED;
+    p->cfg = cfg;
+    auto bail = [&](rtg_status s) {
+        tc_plan_free(p);
+        return s;
+    };
+    const Csr &c = g->ori;
+    const uint32_t E = cfg.tc_item_edges, H = cfg.tc_hash_slots, W = cfg.tc_block_warps;
+    const uint64_t item_cap = c.m / E + c.n + 1;
+    rtg_status s;
+    if ((s = dev_alloc(ctx, (void **)&p->items, item_cap * 8)) != RTG_OK) return bail(s);
+    if ((s = dev_alloc(ctx, (void **)&p->vcnt, (c.n + 1ull) * 4 * 2)) != RTG_OK) return bail(s);
+    if ((s = dev_alloc(ctx, (void **)&p->acc, 8 * sizeof(unsigned long long))) != RTG_OK)
+        return bail(s);
+    uint32_t *vbase = p->vcnt + (c.n + 1ull);
+    size_t cub_bytes = 0;
+    cudaError_t e = cub::DeviceScan::ExclusiveSum(nullptr, cub_bytes, p->vcnt, vbase,
+                                                  (int64_t)c.n + 1, ctx->stream);
+    if (e != cudaSuccess) return bail(cuda_fail(ctx, e, "scan size", __FILE__, __LINE__));
+    if ((s = dev_alloc(ctx, &p->cub_tmp, cub_bytes)) != RTG_OK) return bail(s);
+    if ((e = cudaEventCreate(&p->k0)) != cudaSuccess ||
+        (e = cudaEventCreate(&p->k1)) != cudaSuccess)
+        return bail(cuda_fail(ctx, e, "event", __FILE__, __LINE__));
+
+    const size_t smem = (size_t)W * H * 4;
+    if ((int)smem > ctx->smem_optin)
+        return bail(fail(ctx, RTG_ERR_INVALID_ARG, "schedule needs %zu B of shared memory", smem));
+    if ((e = cudaFuncSetAttribute(k_tc_batched, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)smem)) != cudaSuccess)
+        return bail(cuda_fail(ctx, e, "smem attribute", __FILE__, __LINE__));
+    int per_sm = 0;
+    if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_tc_batched, W * 32,
+                                                           smem)) != cudaSuccess)
+        return bail(cuda_fail(ctx, e, "occupancy", __FILE__, __LINE__));
+    if (cfg.tc_blocks_per_sm) per_sm = std::min<int>(per_sm, (int)cfg.tc_blocks_per_sm);
+    per_sm = std::max(per_sm, 1);
+    const int grid = ctx->sm_count * per_sm;
+    const int g1 = (int)std::max<uint64_t>(1, std::min<uint64_t>((c.n + 256ull) / 256,
+                                                                  ctx->sm_count * 16ull));
+
+    // capture: reset -> item counts -> scan -> item fill -> [ev] persistent count [ev]
+    if ((e = cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal)) !=
+        cudaSuccess)
+        return bail(cuda_fail(ctx, e, "capture", __FILE__, __LINE__));
+    cudaMemsetAsync(p->acc, 0, 8 * sizeof(unsigned long long), ctx->stream);
+    k_item_counts<<<g1, 256, 0, ctx->stream>>>(c.off, c.n, E, p->vcnt);
+    cub::DeviceScan::ExclusiveSum(p->cub_tmp, cub_bytes, p->vcnt, vbase, (int64_t)c.n + 1,
+                                  ctx->stream);
+    k_item_fill<<<g1, 256, 0, ctx->stream>>>(c.off, c.n, E, vbase, p->items, p->acc);
+    cudaEventRecordWithFlags(p->k0, ctx->stream, cudaEventRecordExternal);
+    k_tc_batched<<<grid, W * 32, smem, ctx->stream>>>(c.off, c.adj, p->items, p->acc, E, H);
+    cudaEventRecordWithFlags(p->k1, ctx->stream, cudaEventRecordExternal);
+    e = cudaStreamEndCapture(ctx->stream, &p->graph);
+    if (e != cudaSuccess) return bail(cuda_fail(ctx, e, "end capture", __FILE__, __LINE__));
+    if ((e = cudaGraphInstantiate(&p->exec, p->graph, 0)) != cudaSuccess)
+        return bail(cuda_fail(ctx, e, "instantiate", __FILE__, __LINE__));
+    size_t nn = 0;
+    cudaGraphGetNodes(p->graph, nullptr, &nn);
+    std::vector<cudaGraphNode_t> nodes(nn);
+    cudaGraphGetNodes(p->graph, nodes.data(), &nn);
+    for (auto nd : nodes) {
+        cudaGraphNodeType t;
+        cudaGraphNodeGetType(nd, &t);
+        if (t == cudaGraphNodeTypeKernel) p->graph_kernels++;
+    }
+    g->plan_batched = p;
+    *out = p;
+    return RTG_OK;
+}
+
+rtg_status count_batched(rtg_ctx *ctx, rtg_graph *g, uint64_t *total, rtg_timing *t) {
+    TcPlan *p = nullptr;
+    RTG_TRY(batched_plan(ctx, g, &p));
+    RTG_CUDA(ctx, cudaEventRecord(ctx->ev[0], ctx->stream));
+    RTG_CUDA(ctx, cudaGraphLaunch(p->exec, ctx->stream));
+    RTG_CUDA(ctx, cudaEventRecord(ctx->ev[1], ctx->stream));
+    ctx->launches += p->graph_kernels;
+    unsigned long long h = 0;
+    RTG_CUDA(ctx, cudaMemcpyAsync(&h, p->acc, 8, cudaMemcpyDeviceToHost, ctx->stream));
+    RTG_CUDA(ctx, cudaEventRecord(ctx->ev[2], ctx->stream));
+    RTG_CUDA(ctx, cudaEventSynchronize(ctx->ev[2]));
+    *total = h;
+    float ms = 0, kms = 0, dms = 0;
+    cudaEventElapsedTime(&ms, ctx->ev[0], ctx->ev[1]);
+    cudaEventElapsedTime(&kms, p->k0, p->k1);
+    cudaEventElapsedTime(&dms, ctx->ev[1], ctx->ev[2]);
+    t->count_ms = ms;
+    t->main_kernel_ms = kms;
+    t->d2h_ms += dms;
+    t->kernel_launches += p->graph_kernels;
+    return RTG_OK;
+}
+
+rtg_status count_plain(rtg_ctx *ctx, rtg_graph *g, uint64_t *total, rtg_timing *t) {
+    const Csr &c = g->ori;
+    TcPlan *p = g->plan_plain;
+    if (!p) {
+        p = new TcPlan();
+        p->mode = RTG_TC_PLAIN;
+        rtg_status s = dev_alloc(ctx, (void **)&p->bucket, std::max<uint64_t>(c.m, 1));
+        if (s == RTG_OK) s = dev_alloc(ctx, (void **)&p->lists, std::max<uint64_t>(c.m, 1) * 4);
+        if (s == RTG_OK)
+            s = dev_alloc(ctx, (void **)&p->acc, (1 + 3 * kPlainBuckets) * sizeof(unsigned long long));
+        for (auto &ev : p->bev)
+            if (s == RTG_OK && cudaEventCreate(&ev) != cudaSuccess)
+                s = cuda_fail(ctx, cudaGetLastError(), "event", __FILE__, __LINE__);
+        if (s != RTG_OK) {
+            tc_plan_free(p);
+            return s;
+        }
+        g->plan_plain = p;
+    }
+    uint64_t l0 = ctx->launches;
+    unsigned long long *d_total = p->acc, *d_counts = p->acc + 1, *d_base = d_counts + kPlainBuckets,
+                       *d_cursor = d_base + kPlainBuckets;
+    const int grid = (int)std::max<uint64_t>(1, std::min<uint64_t>((c.m + 255) / 256,
+                                                                    ctx->sm_count * 16ull));
+    RTG_CUDA(ctx, cudaEventRecord(ctx->ev[0], ctx->stream));
+    RTG_CUDA(ctx, cudaMemsetAsync(p->acc, 0, (1 + 3 * kPlainBuckets) * 8, ctx->stream));
+    if (c.m) {
+        k_plain_classify<<<grid, 256, 0, ctx->stream>>>(c.off, c.adj, c.src, c.m, p->bucket,
+                                                        d_counts);
+        ctx->launches++;
+        RTG_CUDA(ctx, cudaGetLastError());
+    }
+    unsigned long long hc[kPlainBuckets] = {0};
+    RTG_CUDA(ctx, cudaMemcpyAsync(hc, d_counts, sizeof hc, cudaMemcpyDeviceToHost, ctx->stream));
+    RTG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    unsigned long long hb[kPlainBuckets], run = 0;
+    for (int i = 0; i < kPlainBuckets; ++i) {
+        hb[i] = run;
+        run += hc[i];
+    }
+    float kms_sum = 0;
+    if (run) {
+        RTG_CUDA(ctx, cudaMemcpyAsync(d_base, hb, sizeof hb, cudaMemcpyHostToDevice, ctx->stream));
+        k_plain_scatter<<<grid, 256, 0, ctx->stream>>>(p->bucket, c.m, d_base, d_cursor, p->lists);
+        ctx->launches++;
+        RTG_CUDA(ctx, cudaGetLastError());
+        for (int i = 0; i < kPlainBuckets; ++i) {
+            if (!hc[i]) continue;
+            uint64_t blocks = (hc[i] + 7) / 8;
+            int gb = (int)std::min<uint64_t>(blocks, 65535);
+            RTG_CUDA(ctx, cudaEventRecord(p->bev[2 * i], ctx->stream));
+            if (i < 3)
+                k_plain_edges<false><<<gb, 256, 0, ctx->stream>>>(c.off, c.adj, c.src,
+                                                                  p->lists + hb[i], hc[i], d_total);
+            else
+                k_plain_edges<true><<<gb, 256, 0, ctx->stream>>>(c.off, c.adj, c.src,
+                                                                 p->lists + hb[i], hc[i], d_total);
+            ctx->launches++;
+            RTG_CUDA(ctx, cudaGetLastError());
+            RTG_CUDA(ctx, cudaEventRecord(p->bev[2 * i + 1], ctx->stream));
+        }
+    }
+    RTG_CUDA(ctx, cudaEventRecord(ctx->ev[1], ctx->stream));
+    unsigned long long h = 0;
+    RTG_CUDA(ctx, cudaMemcpyAsync(&h, d_total, 8, cudaMemcpyDeviceToHost, ctx->stream));
+    RTG_CUDA(ctx, cudaEventRecord(ctx->ev[2], ctx->stream));
+    RTG_CUDA(ctx, cudaEventSynchronize(ctx->ev[2]));
+    *total = h;
+    for (int i = 0; i < kPlainBuckets && run; ++i) {
+        if (!hc[i]) continue;
+        float bms = 0;
+        cudaEventElapsedTime(&bms, p->bev[2 * i], p->bev[2 * i + 1]);
+        kms_sum += bms;
+    }
+    float ms = 0, dms = 0;
+    cudaEventElapsedTime(&ms, ctx->ev[0], ctx->ev[1]);
+    cudaEventElapsedTime(&dms, ctx->ev[1], ctx->ev[2]);
+    t->count_ms = ms;
+    t->main_kernel_ms = kms_sum;
+    t->d2h_ms += dms;
+    t->kernel_launches += ctx->launches - l0;
+    return RTG_OK;
+}
+
+}  // namespace
+
+rtg_status tc_count(rtg_ctx *ctx, rtg_graph *g, rtg_tc_mode mode, uint64_t *total,
+                    rtg_timing *t) {
+    const Csr &c = g->ori;
+    if (c.n > 0x7FFFFFFFu || c.m >= (1ull << 32))
+        return fail(ctx, RTG_ERR_INVALID_ARG, "graph too large for 32-bit edge ids");
+    t->algo_bytes = 4 * c.work_elems + 8 * c.m;
+    if (c.m == 0) {
+        *total = 0;
+        return RTG_OK;
+    }
+    if (mode == RTG_TC_PLAIN) return count_plain(ctx, g, total, t);
+    return count_batched(ctx, g, total, t);
+}
+
+}  // namespace rtg
