@@ -1,0 +1,345 @@
+#!/usr/bin/env python3
+"""Benchmark: exact triangle count of an R-MAT scale-21 graph on one GB300.
+
+Workload (the batched-TC configuration): R-MAT scale 21, edge factor 16 (2^25 samples),
+(a,b,c,d) = (0.57,0.19,0.19,0.05), seed 42, symmetrised, deduplicated, self loops removed,
+oriented by degree. A step is one exact uint64 count of the resident CSR:
+
+  value   – edges/s = m / device time of the BATCHED count (persistent kernel in a CUDA
+            graph), CSR resident in HBM, L2 flushed before every step (CUDA events).
+  e2e     – the same metric through the public C ABI with host buffers:
+            rtg_tc_count_host_edges (pinned host edges -> H2D -> GPU CSR build -> count ->
+            D2H of the total), wall time per call.
+  plain   – the PLAIN form (one launch per bucket) on the same CSR, for the batched/plain
+            ratio.
+  roofline– the persistent kernel's algorithmic bytes (4 * sum over oriented edges of
+            (d+(u) + d+(v)) + 8 m) / its CUDA-event duration vs the measured HBM peak.
+  cpu_baseline – the oracle's restatement of the reference's ListIntersectionKernel
+            (bs_tc.cu:120-148) on the host cores, on a stride sample of source vertices.
+
+`--impl reference` runs only the reference's CPU algorithm (oracle port; the reference's
+own code cannot be built on the benchmark host) on the same workload and prints its line.
+With torchrun (N>1) every rank runs an independent replica on its own GPU (the count does
+not shard across GPUs here); rank 0 prints one line with the max time over ranks.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+REPO = Path(__file__).resolve().parent
+sys.path.insert(0, str(REPO / "rt-graph_gb300"))
+sys.path.insert(0, str(REPO))
+
+WORKLOAD = dict(workload="rmat21_ef16_tc", scale=21, edge_factor=16, abcd=[0.57, 0.19, 0.19, 0.05],
+                seed=42, orientation="degree (post-dedup)", counter="uint64")
+METRIC = "TC edges/s"
+UNIT = "edges/s"
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+class Dist:
+    """Barrier / max / sum across ranks (torch.distributed when WORLD_SIZE > 1)."""
+
+    def __init__(self, backend: str | None = None):
+        self.ws, self.rank, self.local = dist_env()
+        self.pg = None
+        if self.ws > 1:
+            import torch.distributed as td
+            td.init_process_group(backend=backend or "gloo")
+            self.td = td
+
+    def barrier(self):
+        if self.ws > 1:
+            self.td.barrier()
+
+    def reduce(self, x: float, op: str) -> float:
+        if self.ws == 1:
+            return x
+        import torch
+        t = torch.tensor([x], dtype=torch.float64)
+        self.td.all_reduce(t, op=self.td.ReduceOp.MAX if op == "max" else self.td.ReduceOp.SUM)
+        return float(t.item())
+
+    def close(self):
+        if self.ws > 1:
+            self.td.destroy_process_group()
+
+
+def aggregate(dist: Dist, units_local: float, ms_local: float) -> tuple[float, float]:
+    """Whole-job throughput: units of all ranks / the slowest rank's time."""
+    ms = dist.reduce(ms_local, "max")
+    units = dist.reduce(units_local, "sum")
+    return units / (ms / 1e3), ms
+
+
+class ClockSampler:
+    """nvidia-smi samples during the timed region (SM clock, throttle reasons)."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu: int):
+        self.gpu = gpu
+        self.proc = None
+        self.lines: list[str] = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except (FileNotFoundError, OSError):
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self) -> dict:
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.lines:
+            p = [x.strip() for x in line.split(",")]
+            if len(p) < 9:
+                continue
+            try:
+                sm.append(float(p[1]))
+                mx = float(p[2])
+            except ValueError:
+                continue
+            for name, flag in zip(names, p[5:9]):
+                if flag.lower() == "active":
+                    reasons.add(name)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        loaded = [x for x in sm if mx and x > 0.5 * mx] or sm
+        return {"sm_mhz": statistics.median(loaded), "sm_max_mhz": mx,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_peaks() -> dict:
+    p = REPO / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return {"hbm_gbs": d["hbm_gbs"], "source": "measured"}
+    return {"hbm_gbs": 6800.0, "source": "fallback"}
+
+
+def profile_traffic(name: str):
+    """DRAM bytes per launch of the dominant kernel from a committed ncu summary."""
+    p = REPO / "profiles" / f"{name}.txt"
+    if not p.exists():
+        return None
+    for line in p.read_text().splitlines():
+        if line.startswith("dram_bytes_per_full_launch:"):
+            return int(float(line.split(":")[1]))
+    return None
+
+
+def gen_workload():
+    import rtg
+    return rtg.gen_rmat(WORKLOAD["scale"], WORKLOAD["edge_factor"], *WORKLOAD["abcd"][:3],
+                        seed=WORKLOAD["seed"])
+
+
+def cpu_baseline_tc(off: np.ndarray, adj: np.ndarray, target_s: float = 15.0) -> dict:
+    """The oracle's ListIntersectionKernel restatement on a stride sample of source
+    vertices, all host threads. Returns edges/s on the sampled oriented edges."""
+    import oracle
+    n = len(off) - 1
+    threads = os.cpu_count() or 1
+    off32 = off.astype(np.int32)
+    adj32 = adj.astype(np.int32)
+    stride = 256
+    while True:
+        rows = np.arange(0, n, stride, dtype=np.int32)
+        edges = int((off32[rows + 1] - off32[rows]).sum())
+        t0 = time.perf_counter()
+        oracle.tc_bsearch_rows(off32, adj32, rows, threads)
+        dt = time.perf_counter() - t0
+        if dt * 4 > target_s or stride == 1:
+            break
+        stride = max(1, stride // 4)
+    return {"value": edges / dt, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"every {stride}-th source vertex ({edges} oriented edges, {dt:.1f} s), "
+                      "ListIntersectionKernel restatement (per edge x binary search), OpenMP"}
+
+
+def run_reference(args, dist: Dist) -> None:
+    if dist.rank != 0:
+        return
+    import oracle
+    s, d = gen_workload()
+    off, adj = oracle.degree_csr(s, d)
+    m = len(adj)
+    off32, adj32 = off.astype(np.int32), adj.astype(np.int32)
+    n = len(off) - 1
+    threads = os.cpu_count() or 1
+    stride = args.ref_stride
+    rows = np.arange(0, n, stride).astype(np.int32)
+    sampled_edges = int((off32[rows + 1] - off32[rows]).sum())
+    for _ in range(args.warmup):
+        oracle.tc_bsearch_rows(off32, adj32, rows[: max(1, len(rows) // 50)], threads)
+    times = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        oracle.tc_bsearch_rows(off32, adj32, rows, threads)
+        times.append(time.perf_counter() - t0)
+    ms = 1e3 * sum(times) / len(times)
+    value = sampled_edges / (ms / 1e3)
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u32",
+            "data": "synthetic (seeded R-MAT)", "impl": "reference",
+            "config": dict(WORKLOAD, m=m, sample_stride=stride, sampled_edges=sampled_edges),
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+                             "sample": f"every {stride}-th source vertex, {sampled_edges} "
+                                       "oriented edges per step; restatement of the reference's "
+                                       "ListIntersectionKernel (tc/bs_tc/bs_tc.cu:120-148)"},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def run_gpu(args, dist: Dist) -> None:
+    import rtg
+    ctx = rtg.Context(dist.local if dist.ws > 1 else 0)
+    s, d = gen_workload()
+    g = ctx.graph_from_edges(s, d).build(rtg.ORIENT_DEGREE)
+    g.release_edges()
+    info = g.info()
+    m = info.m
+    # warm-up (also builds and captures the CUDA graph of the batched count)
+    for _ in range(args.warmup):
+        ctx.flush_l2()
+        g.tc(rtg.TC_BATCHED)
+        g.tc(rtg.TC_PLAIN)
+    want = g.tc(rtg.TC_BATCHED)[0]
+    # ---- timed region: batched count, L2 flushed between steps
+    launches0 = ctx.launches
+    ms_steps, kms_steps = [], []
+    dist.barrier()
+    ctx.sync()
+    with ClockSampler(dist.local) as clk:
+        for _ in range(args.steps):
+            ctx.flush_l2()
+            total, t = g.tc(rtg.TC_BATCHED)
+            if total != want:
+                raise RuntimeError(f"count changed between steps: {total} != {want}")
+            ms_steps.append(t.count_ms)
+            kms_steps.append(t.main_kernel_ms)
+        ctx.sync()
+    dist.barrier()
+    launches = ctx.launches - launches0 - args.steps  # flushes are memsets, not kernels
+    algo_bytes = t.algo_bytes
+    ms_local = sum(ms_steps) / len(ms_steps)
+    value, ms = aggregate(dist, m, ms_local)
+    # ---- plain form on the same CSR
+    plain_ms = []
+    for _ in range(args.steps):
+        ctx.flush_l2()
+        tp, t2 = g.tc(rtg.TC_PLAIN)
+        if tp != want:
+            raise RuntimeError("plain count differs from batched count")
+        plain_ms.append(t2.count_ms)
+    plain_value, _ = aggregate(dist, m, sum(plain_ms) / len(plain_ms))
+    # ---- end to end through the C ABI with pinned host buffers
+    hs = ctx.host_array(len(s), np.uint32)
+    hd = ctx.host_array(len(d), np.uint32)
+    hs[:] = s
+    hd[:] = d
+    ctx.tc_count_host_edges(hs, hd, rtg.ORIENT_DEGREE, rtg.TC_BATCHED)  # warm
+    e2e_ms = []
+    for _ in range(max(1, min(args.steps, 5))):
+        t0 = time.perf_counter()
+        tot, te = ctx.tc_count_host_edges(hs, hd, rtg.ORIENT_DEGREE, rtg.TC_BATCHED)
+        e2e_ms.append((time.perf_counter() - t0) * 1e3)
+        if tot != want:
+            raise RuntimeError("end-to-end count differs")
+    e2e_value, _ = aggregate(dist, m, sum(e2e_ms) / len(e2e_ms))
+    kms = sum(kms_steps) / len(kms_steps)
+    peaks = measured_peaks()
+    achieved = algo_bytes / (kms / 1e3) / 1e9
+    roofline = {"bound": "hbm", "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",
+                "frac": achieved / peaks["hbm_gbs"], "traffic": profile_traffic("tc_batched_rmat21"),
+                "peak_source": peaks["source"], "kernel": "k_tc_batched",
+                "kernel_ms": kms, "algo_bytes_per_launch": algo_bytes}
+    cpu = None
+    if dist.rank == 0 and dist.ws == 1 and not args.no_cpu_baseline:
+        off, adj = g.csr()
+        cpu = cpu_baseline_tc(off, adj)
+    if dist.rank == 0:
+        line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": dist.ws,
+                "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u32",
+                "data": "synthetic (seeded R-MAT, generated on the host)",
+                "config": dict(WORKLOAD, n=info.n, m=m, m_input=info.m_input,
+                               max_out_degree=info.max_out_degree, triangles=want,
+                               mode="batched", l2="flushed before every step",
+                               timing="CUDA events around each count on the context stream",
+                               parallelism="replicas" if dist.ws > 1 else "single GPU"),
+                "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(te.h2d_bytes),
+                        "d2h_bytes_per_step": int(te.d2h_bytes),
+                        "ms_per_step": sum(e2e_ms) / len(e2e_ms),
+                        "api": "rtg_tc_count_host_edges (pinned host edges, CSR build included)"},
+                "plain": {"value": plain_value, "unit": UNIT,
+                          "ms_per_step": sum(plain_ms) / len(plain_ms)},
+                "batched_over_plain": value / plain_value,
+                "roofline": roofline, "cpu_baseline": cpu, "clocks": clk.summary(),
+                "gpu_launches": int(launches)}
+        print(json.dumps(line), flush=True)
+    ctx.close()
+
+
+def main() -> None:
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="rtg", choices=["rtg", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--ref-stride", type=int, default=32)
+    args = ap.parse_args()
+    if args.warmup < 3:
+        ap.error("at least 3 warm-up steps")
+    dist = Dist("gloo" if args.impl == "reference" else None)
+    try:
+        if args.impl == "reference":
+            run_reference(args, dist)
+        else:
+            run_gpu(args, dist)
+    finally:
+        dist.close()
+
+
+if __name__ == "__main__":
+    main()

@@ -132,9 +132,12 @@ typedef struct rtg_graph_info {
  * any field means "library default". */
 typedef struct rtg_config {
     uint32_t tc_block_warps;    /* warps per block of the persistent TC kernel        */
-    uint32_t tc_item_edges;     /* oriented edges per work item                       */
-    uint32_t tc_hash_slots;     /* shared-memory hash slots per warp (power of two)   */
+    uint32_t tc_item_edges;     /* in-edges of one vertex per work item               */
+    uint32_t tc_hash_slots;     /* shared-memory hash slots per block (power of two;
+                                   0 = 4x the longest out-list, within [1024, 16384]) */
     uint32_t tc_blocks_per_sm;  /* resident blocks per SM of the persistent kernel    */
+    uint32_t tc_stage_slots;    /* bulk-copy staging slots per warp (2..16)           */
+    uint32_t tc_stage_bytes;    /* bytes per staging slot (multiple of 128, >= 256)   */
     uint32_t si_block_warps;    /* warps per block of the SI kernels                  */
     uint32_t si_search_ratio;   /* long/short length ratio above which SEARCH is used */
     uint32_t si_split_len;      /* pairs with |A|+|B| above this are split by merge
@@ -144,6 +147,8 @@ typedef struct rtg_config {
 
 /* ---------------------------------------------------------------- context */
 rtg_status rtg_init(int device, rtg_ctx **out);
+/* Also releases every graph and set collection still attached to the context; their
+ * handles are invalid afterwards. */
 void rtg_destroy(rtg_ctx *ctx);
 const char *rtg_last_error(const rtg_ctx *ctx);
 const char *rtg_status_str(rtg_status s);

@@ -20,7 +20,11 @@ LIB_PATH = HERE / "_build" / "liboracle.so"
 
 
 def _load():
-    if not LIB_PATH.exists():
+    src = HERE / "rtg_oracle.c"
+    stale = (not LIB_PATH.exists() or
+             max(src.stat().st_mtime, (HERE / "rtg_oracle.h").stat().st_mtime)
+             > LIB_PATH.stat().st_mtime)
+    if stale:
         import subprocess
         LIB_PATH.parent.mkdir(parents=True, exist_ok=True)
         subprocess.run(["gcc", "-O3", "-fPIC", "-shared", "-fopenmp", "-std=c11",
@@ -34,6 +38,7 @@ def _load():
         "orc_csr_symmetric": (C.c_int, [P, P, C.c_uint64, C.c_uint32, P, P, P]),
         "orc_tc_bsearch_i32": (C.c_uint64, [P, P, C.c_int32, C.c_int]),
         "orc_tc_hashmap_i32": (C.c_uint64, [P, P, C.c_int32, C.c_int]),
+        "orc_tc_bsearch_rows": (C.c_uint64, [P, P, P, C.c_int64, C.c_int]),
         "orc_tc_merge": (C.c_uint64, [P, P, C.c_uint32, C.c_int]),
         "orc_si_merge": (C.c_uint32, [P, C.c_uint32, P, C.c_uint32]),
         "orc_si_bsearch": (C.c_uint32, [P, C.c_uint32, P, C.c_uint32]),
@@ -103,6 +108,13 @@ def tc_bsearch_i32(off: np.ndarray, adj: np.ndarray, threads: int = 0) -> int:
     off = np.ascontiguousarray(off, np.int32)
     adj = np.ascontiguousarray(adj, np.int32)
     return lib.orc_tc_bsearch_i32(_p(off), _p(adj), len(off) - 1, threads)
+
+
+def tc_bsearch_rows(off: np.ndarray, adj: np.ndarray, rows: np.ndarray, threads: int = 0) -> int:
+    off = np.ascontiguousarray(off, np.int32)
+    adj = np.ascontiguousarray(adj, np.int32)
+    rows = np.ascontiguousarray(rows, np.int32)
+    return lib.orc_tc_bsearch_rows(_p(off), _p(adj), _p(rows), len(rows), threads)
 
 
 def tc_hashmap_i32(off: np.ndarray, adj: np.ndarray, threads: int = 0) -> int:

@@ -207,6 +207,27 @@ uint64_t orc_tc_bsearch_i32(const int32_t *offsets, const int32_t *adjs, int32_t
     return total;
 }
 
+uint64_t orc_tc_bsearch_rows(const int32_t *offsets, const int32_t *adjs, const int32_t *rows,
+                             int64_t nrows, int threads) {
+    set_threads(threads);
+    uint64_t total = 0;
+    /* bs_tc.cu:120-148 restricted to the oriented edges whose source is listed in rows */
+#pragma omp parallel for schedule(dynamic, 16) reduction(+ : total)
+    for (int64_t r = 0; r < nrows; ++r) {
+        int32_t u = rows[r];
+        for (int32_t e = offsets[u]; e < offsets[u + 1]; ++e) {
+            int32_t w = adjs[e];
+            for (int32_t i = offsets[u]; i < offsets[u + 1]; ++i) {
+                int32_t v = adjs[i];
+                int32_t len = offsets[v + 1] - offsets[v];
+                if (len == 0) continue;
+                total += binary_check(adjs + offsets[v], 0, len - 1, w);
+            }
+        }
+    }
+    return total;
+}
+
 static int cmp_i32(const void *x, const void *y) {
     int32_t a = *(const int32_t *)x, b = *(const int32_t *)y;
     return a < b ? -1 : (a > b ? 1 : 0);

@@ -44,6 +44,11 @@ int orc_csr_symmetric(const uint32_t *src, const uint32_t *dst, uint64_t m, uint
 uint64_t orc_tc_bsearch_i32(const int32_t *offsets, const int32_t *adjs, int32_t nodes,
                             int threads);
 
+/* The same rule restricted to the oriented edges whose source vertex is in rows[0..nrows):
+ * the bounded sample used as the timed CPU baseline. */
+uint64_t orc_tc_bsearch_rows(const int32_t *offsets, const int32_t *adjs, const int32_t *rows,
+                             int64_t nrows, int threads);
+
 /* tc/bs_tc/bs_tc.cu:153-211 (Preprocessing: per-vertex two-hop aggregation into
  * (u, w, cnt) triples) and :213-229 (HashmapKernel: add cnt when w in N+(u)). */
 uint64_t orc_tc_hashmap_i32(const int32_t *offsets, const int32_t *adjs, int32_t nodes,

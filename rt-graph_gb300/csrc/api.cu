@@ -84,6 +84,14 @@ rtg_status graph_free_csr(Csr &c) {
     return RTG_OK;
 }
 
+void count_csr_free(CountCsr &cc) {
+    dev_free(cc.off);
+    dev_free(cc.adj);
+    dev_free(cc.in_off);
+    dev_free(cc.in_rng);
+    cc = CountCsr{};
+}
+
 }  // namespace rtg
 
 using namespace rtg;
@@ -153,6 +161,9 @@ void rtg_destroy(rtg_ctx *ctx) {
     if (!ctx) return;
     cudaSetDevice(ctx->device);
     cudaStreamSynchronize(ctx->stream);
+    // release what the caller did not: graphs and set collections die with their context
+    while (!ctx->graphs.empty()) rtg_graph_destroy(*ctx->graphs.begin());
+    while (!ctx->sets.empty()) rtg_sets_destroy(*ctx->sets.begin());
     for (auto &b : ctx->scratch) dev_free(b.ptr);
     dev_free(ctx->flush_buf);
     dev_free(ctx->d_status);
@@ -167,10 +178,16 @@ rtg_status rtg_set_config(rtg_ctx *ctx, const rtg_config *cfg) {
     if (!ctx || !cfg) return RTG_ERR_INVALID_ARG;
     if (cfg->tc_hash_slots && (cfg->tc_hash_slots & (cfg->tc_hash_slots - 1)))
         return fail(ctx, RTG_ERR_INVALID_ARG, "tc_hash_slots must be a power of two");
-    if (cfg->tc_hash_slots && (cfg->tc_hash_slots < 64 || cfg->tc_hash_slots > 8192))
-        return fail(ctx, RTG_ERR_INVALID_ARG, "tc_hash_slots must be in [64, 8192]");
+    if (cfg->tc_hash_slots && (cfg->tc_hash_slots < 64 || cfg->tc_hash_slots > 16384))
+        return fail(ctx, RTG_ERR_INVALID_ARG, "tc_hash_slots must be in [64, 16384]");
     if (cfg->tc_block_warps > 32 || cfg->si_block_warps > 32)
         return fail(ctx, RTG_ERR_INVALID_ARG, "at most 32 warps per block");
+    if (cfg->tc_stage_slots && (cfg->tc_stage_slots < 2 || cfg->tc_stage_slots > 16))
+        return fail(ctx, RTG_ERR_INVALID_ARG, "tc_stage_slots must be in [2, 16]");
+    if (cfg->tc_stage_bytes && (cfg->tc_stage_bytes < 256 || cfg->tc_stage_bytes % 128 ||
+                                cfg->tc_stage_bytes > 65536))
+        return fail(ctx, RTG_ERR_INVALID_ARG,
+                    "tc_stage_bytes must be a multiple of 128 in [256, 65536]");
     ctx->cfg = *cfg;
     return RTG_OK;
 }
@@ -226,9 +243,15 @@ void rtg_host_free(void *p) {
 
 /* ------------------------------------------------------------------ graphs */
 
-static rtg_status new_graph_device_edges(rtg_ctx *ctx, uint64_t m, rtg_graph **out) {
+static rtg_graph *new_graph(rtg_ctx *ctx) {
     rtg_graph *g = new rtg_graph();
     g->ctx = ctx;
+    ctx->graphs.insert(g);
+    return g;
+}
+
+static rtg_status new_graph_device_edges(rtg_ctx *ctx, uint64_t m, rtg_graph **out) {
+    rtg_graph *g = new_graph(ctx);
     g->m_input = m;
     rtg_status s = dev_alloc(ctx, (void **)&g->d_src, m * sizeof(uint32_t));
     if (s == RTG_OK) s = dev_alloc(ctx, (void **)&g->d_dst, m * sizeof(uint32_t));
@@ -306,7 +329,17 @@ rtg_status rtg_csr_build(rtg_ctx *ctx, rtg_graph *g, rtg_orient orient) {
         return fail(ctx, RTG_ERR_INVALID_ARG, "unknown orientation %d", (int)orient);
     if (g->edges_released)
         return fail(ctx, RTG_ERR_STATE, "raw edges were released; cannot build a CSR");
-    return build_csr(ctx, g, orient);
+    if (orient != RTG_ORIENT_SYMMETRIC) {
+        // cached counting plans point into the CSR about to be replaced
+        cudaStreamSynchronize(ctx->stream);
+        tc_plan_free(g->plan_batched);
+        tc_plan_free(g->plan_plain);
+        g->plan_batched = g->plan_plain = nullptr;
+        count_csr_free(g->cnt);
+    }
+    RTG_TRY(build_csr(ctx, g, orient));
+    if (orient != RTG_ORIENT_SYMMETRIC) RTG_TRY(csr_build_count(ctx, g->ori, g->cnt));
+    return RTG_OK;
 }
 
 rtg_status rtg_graph_info_get(const rtg_graph *g, rtg_graph_info *info) {
@@ -368,18 +401,24 @@ uint64_t rtg_graph_device_bytes(const rtg_graph *g) {
         if (!c.built) return 0;
         return (uint64_t)(c.n + 1) * 8 + c.m * 4 + (c.src ? c.m * 4 : 0);
     };
-    return b + csr_bytes(g->ori) + csr_bytes(g->sym);
+    const CountCsr &cc = g->cnt;
+    uint64_t cb = cc.built ? (uint64_t)(cc.n + 1) * 16 + cc.m * 12 : 0;
+    return b + csr_bytes(g->ori) + csr_bytes(g->sym) + cb;
 }
 
 void rtg_graph_destroy(rtg_graph *g) {
     if (!g) return;
-    if (g->ctx) cudaStreamSynchronize(g->ctx->stream);
+    if (g->ctx) {
+        cudaStreamSynchronize(g->ctx->stream);
+        g->ctx->graphs.erase(g);
+    }
     tc_plan_free(g->plan_batched);
     tc_plan_free(g->plan_plain);
     dev_free(g->d_src);
     dev_free(g->d_dst);
     graph_free_csr(g->ori);
     graph_free_csr(g->sym);
+    count_csr_free(g->cnt);
     delete g;
 }
 
@@ -441,8 +480,7 @@ rtg_status rtg_graph_from_host_csr(rtg_ctx *ctx, const int32_t *offsets, const i
     *out = nullptr;
     if (offsets[nodes] != edges || offsets[0] != 0)
         return fail(ctx, RTG_ERR_INVALID_ARG, "offsets[0] must be 0 and offsets[nodes] == edges");
-    rtg_graph *g = new rtg_graph();
-    g->ctx = ctx;
+    rtg_graph *g = new_graph(ctx);
     g->m_input = (uint64_t)edges;
     g->edges_released = true;
     Csr &c = g->ori;
@@ -457,7 +495,7 @@ rtg_status rtg_graph_from_host_csr(rtg_ctx *ctx, const int32_t *offsets, const i
         return st;
     };
     if ((s = dev_alloc(ctx, (void **)&c.off, (c.n + 1) * 8ull)) != RTG_OK) return cleanup(s);
-    if ((s = dev_alloc(ctx, (void **)&c.adj, c.m * 4)) != RTG_OK) return cleanup(s);
+    if ((s = dev_alloc(ctx, (void **)&c.adj, c.m * 4 + kAdjPadBytes)) != RTG_OK) return cleanup(s);
     if ((s = dev_alloc(ctx, (void **)&c.src, c.m * 4)) != RTG_OK) return cleanup(s);
     if ((s = dev_alloc(ctx, (void **)&d_off32, (c.n + 1) * 4ull)) != RTG_OK) return cleanup(s);
     if ((s = dev_alloc(ctx, (void **)&d_adj32, c.m * 4)) != RTG_OK) return cleanup(s);
@@ -491,6 +529,7 @@ rtg_status rtg_graph_from_host_csr(rtg_ctx *ctx, const int32_t *offsets, const i
     c.work_elems = hw[0];
     c.max_deg = (uint32_t)hw[1];
     c.built = true;
+    if ((s = csr_build_count(ctx, c, g->cnt)) != RTG_OK) return cleanup(s);
     g->orient = RTG_ORIENT_DEGREE_RAW_REF;
     *out = g;
     return cleanup(RTG_OK);
@@ -613,6 +652,7 @@ rtg_status rtg_sets_from_host(rtg_ctx *ctx, const uint64_t *offsets, uint64_t ns
     if (ne && !elems) return RTG_ERR_INVALID_ARG;
     rtg_sets *s = new rtg_sets();
     s->ctx = ctx;
+    ctx->sets.insert(s);
     s->nsets = nsets;
     s->nelems = ne;
     rtg_status st = dev_alloc(ctx, (void **)&s->off, (nsets + 1) * 8);
@@ -650,7 +690,10 @@ uint64_t rtg_sets_elems(const rtg_sets *s) { return s ? s->nelems : 0; }
 
 void rtg_sets_destroy(rtg_sets *s) {
     if (!s) return;
-    if (s->ctx) cudaStreamSynchronize(s->ctx->stream);
+    if (s->ctx) {
+        cudaStreamSynchronize(s->ctx->stream);
+        s->ctx->sets.erase(s);
+    }
     if (!s->borrowed) {
         dev_free(s->off);
         dev_free(s->elems);

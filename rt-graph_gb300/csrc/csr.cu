@@ -235,7 +235,8 @@ rtg_status fill_csr(rtg_ctx *ctx, const uint64_t *keys, uint64_t m, int B, uint3
     c.n = n;
     c.m = m;
     RTG_TRY(dev_alloc(ctx, (void **)&c.off, (n + 1ull) * 8));
-    RTG_TRY(dev_alloc(ctx, (void **)&c.adj, m * 4));
+    RTG_TRY(dev_alloc(ctx, (void **)&c.adj, m * 4 + kAdjPadBytes));
+    RTG_CUDA(ctx, cudaMemsetAsync((char *)c.adj + m * 4, 0, kAdjPadBytes, ctx->stream));
     if (with_src) RTG_TRY(dev_alloc(ctx, (void **)&c.src, m * 4));
     if (m == 0) {
         RTG_CUDA(ctx, cudaMemsetAsync(c.off, 0, (n + 1ull) * 8, ctx->stream));
@@ -298,7 +299,143 @@ rtg_status simple_keys(rtg_ctx *ctx, rtg_graph *g, uint32_t maxid, int B, uint64
     return RTG_OK;
 }
 
+// ---- counting form: rank relabel + in-edge suffix ranges
+__global__ void k_total_degree(const uint64_t *off, const uint32_t *adj, uint64_t m, uint32_t n,
+                               uint32_t *tdeg) {
+    GRID_STRIDE(v, (uint64_t)n) { atomicAdd(&tdeg[v], (uint32_t)(off[v + 1] - off[v])); }
+    GRID_STRIDE(e, m) { atomicAdd(&tdeg[adj[e]], 1u); }
+}
+
+__global__ void k_rank_keys(const uint32_t *tdeg, uint32_t n, int B, uint64_t *keys) {
+    GRID_STRIDE(v, (uint64_t)n) { keys[v] = ((uint64_t)tdeg[v] << B) | v; }
+}
+
+__global__ void k_rank_scatter(const uint64_t *sorted, uint32_t n, int B, uint32_t *rank) {
+    const uint64_t mask = (1ull << B) - 1;
+    GRID_STRIDE(i, (uint64_t)n) { rank[sorted[i] & mask] = (uint32_t)i; }
+}
+
+// edge keys in rank ids, lower rank first; self loops become the sentinel (n << B)
+__global__ void k_rank_edge_keys(const uint32_t *src, const uint32_t *adj, uint64_t m,
+                                 const uint32_t *rank, int B, uint64_t sentinel, uint64_t *keys) {
+    GRID_STRIDE(e, m) {
+        uint32_t a = rank[src[e]], b = rank[adj[e]];
+        keys[e] = (a == b) ? sentinel : (((uint64_t)min(a, b) << B) | max(a, b));
+    }
+}
+
+// in-edge keys: head rank in the high word, position of the edge in the low word
+__global__ void k_in_keys(const uint32_t *adj_r, uint64_t m, uint64_t *keys) {
+    GRID_STRIDE(e, m) { keys[e] = ((uint64_t)adj_r[e] << 32) | (uint32_t)e; }
+}
+
+__global__ void k_in_fill(const uint64_t *keys, uint64_t m, uint32_t n, const uint64_t *off_r,
+                          const uint32_t *src_r, uint2 *rng, uint64_t *in_off) {
+    GRID_STRIDE(i, m) {
+        const uint64_t k = keys[i];
+        const uint32_t v = (uint32_t)(k >> 32), e = (uint32_t)k;
+        rng[i] = make_uint2(e + 1, (uint32_t)off_r[src_r[e] + 1]);
+        const int64_t prev = (i == 0) ? -1 : (int64_t)(keys[i - 1] >> 32);
+        for (int64_t x = prev + 1; x <= (int64_t)v; ++x) in_off[x] = i;
+        if (i == m - 1)
+            for (uint64_t x = (uint64_t)v + 1; x <= n; ++x) in_off[x] = m;
+    }
+}
+
 }  // namespace
+
+rtg_status csr_build_count(rtg_ctx *ctx, const Csr &c, CountCsr &cc) {
+    count_csr_free(cc);
+    const uint64_t m = c.m;
+    const uint32_t n = c.n;
+    cc.n = n;
+    RTG_TRY(dev_alloc(ctx, (void **)&cc.off, (n + 1ull) * 8));
+    RTG_TRY(dev_alloc(ctx, (void **)&cc.in_off, (n + 1ull) * 8));
+    RTG_TRY(dev_alloc(ctx, (void **)&cc.adj, m * 4 + kAdjPadBytes));
+    RTG_TRY(dev_alloc(ctx, (void **)&cc.in_rng, m * 8 + 16));
+    RTG_CUDA(ctx, cudaMemsetAsync((char *)cc.adj + m * 4, 0, kAdjPadBytes, ctx->stream));
+    if (m == 0 || n == 0) {
+        RTG_CUDA(ctx, cudaMemsetAsync(cc.off, 0, (n + 1ull) * 8, ctx->stream));
+        RTG_CUDA(ctx, cudaMemsetAsync(cc.in_off, 0, (n + 1ull) * 8, ctx->stream));
+        cc.m = 0;
+        cc.built = true;
+        return RTG_OK;
+    }
+    Buffers buf{ctx, {}};
+    const int B = bits_for(n);
+    uint32_t *tdeg, *rank, *src_r;
+    uint64_t *k0, *k1;
+    RTG_TRY(buf.alloc(&tdeg, n));
+    RTG_TRY(buf.alloc(&rank, n));
+    RTG_TRY(buf.alloc(&src_r, m));
+    RTG_TRY(buf.alloc(&k0, std::max<uint64_t>(m, n)));
+    RTG_TRY(buf.alloc(&k1, std::max<uint64_t>(m, n)));
+    RTG_CUDA(ctx, cudaMemsetAsync(tdeg, 0, n * 4ull, ctx->stream));
+    k_total_degree<<<grid_for(ctx, m + n), kThreads, 0, ctx->stream>>>(c.off, c.adj, m, n, tdeg);
+    k_rank_keys<<<grid_for(ctx, n), kThreads, 0, ctx->stream>>>(tdeg, n, B, k0);
+    ctx->launches += 2;
+    RTG_CUDA(ctx, cudaGetLastError());
+    cub::DoubleBuffer<uint64_t> dr(k0, k1);
+    RTG_TRY(radix_sort(ctx, dr, n, std::min(64, B + 32)));
+    k_rank_scatter<<<grid_for(ctx, n), kThreads, 0, ctx->stream>>>(dr.Current(), n, B, rank);
+    const uint64_t sentinel = (uint64_t)n << B;
+    k_rank_edge_keys<<<grid_for(ctx, m), kThreads, 0, ctx->stream>>>(c.src, c.adj, m, rank, B,
+                                                                      sentinel, k0);
+    ctx->launches += 2;
+    RTG_CUDA(ctx, cudaGetLastError());
+    cub::DoubleBuffer<uint64_t> de(k0, k1);
+    RTG_TRY(radix_sort(ctx, de, m, std::min(64, 2 * B)));
+    // duplicates and self loops cannot occur in a CSR built here; a caller-given CSR is
+    // cleaned the same way
+    int64_t *d_num = (int64_t *)(ctx->d_scalars + 4);
+    size_t bytes = 0;
+    RTG_CUDA(ctx, cub::DeviceSelect::Unique(nullptr, bytes, de.Current(), de.Alternate(), d_num,
+                                            (int64_t)m, ctx->stream));
+    void *tmp = nullptr;
+    RTG_TRY(scratch(ctx, 0, bytes, &tmp));
+    RTG_CUDA(ctx, cub::DeviceSelect::Unique(tmp, bytes, de.Current(), de.Alternate(), d_num,
+                                            (int64_t)m, ctx->stream));
+    ctx->launches += 2;
+    int64_t mu = 0;
+    RTG_CUDA(ctx, cudaMemcpyAsync(&mu, d_num, 8, cudaMemcpyDeviceToHost, ctx->stream));
+    RTG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    uint64_t *ek = de.Alternate(), *other = de.Current();
+    if (mu > 0) {
+        uint64_t last = 0;
+        RTG_CUDA(ctx, cudaMemcpy(&last, ek + mu - 1, 8, cudaMemcpyDeviceToHost));
+        if (last == sentinel) --mu;
+    }
+    const uint64_t mr = (uint64_t)mu;
+    cc.m = mr;
+    if (mr == 0) {
+        RTG_CUDA(ctx, cudaMemsetAsync(cc.off, 0, (n + 1ull) * 8, ctx->stream));
+        RTG_CUDA(ctx, cudaMemsetAsync(cc.in_off, 0, (n + 1ull) * 8, ctx->stream));
+        cc.built = true;
+        return RTG_OK;
+    }
+    k_csr_fill<<<grid_for(ctx, mr), kThreads, 0, ctx->stream>>>(ek, mr, B, n, cc.adj, src_r, cc.off);
+    k_in_keys<<<grid_for(ctx, mr), kThreads, 0, ctx->stream>>>(cc.adj, mr, other);
+    ctx->launches += 2;
+    RTG_CUDA(ctx, cudaGetLastError());
+    cub::DoubleBuffer<uint64_t> di(other, ek);
+    RTG_TRY(radix_sort(ctx, di, mr, std::min(64, 32 + B)));
+    k_in_fill<<<grid_for(ctx, mr), kThreads, 0, ctx->stream>>>(di.Current(), mr, n, cc.off, src_r,
+                                                                cc.in_rng, cc.in_off);
+    ctx->launches++;
+    RTG_CUDA(ctx, cudaGetLastError());
+    unsigned long long *w = ctx->d_scalars;
+    RTG_CUDA(ctx, cudaMemsetAsync(w, 0, 16, ctx->stream));
+    k_stats<<<grid_for(ctx, n), kThreads, 0, ctx->stream>>>(cc.off, cc.adj, nullptr, mr, n, w,
+                                                             (unsigned int *)(w + 1));
+    ctx->launches++;
+    RTG_CUDA(ctx, cudaGetLastError());
+    unsigned long long h[2];
+    RTG_CUDA(ctx, cudaMemcpyAsync(h, w, 16, cudaMemcpyDeviceToHost, ctx->stream));
+    RTG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));  // temporaries are freed on return
+    cc.max_deg = (uint32_t)h[1];
+    cc.built = true;
+    return RTG_OK;
+}
 
 rtg_status build_csr(rtg_ctx *ctx, rtg_graph *g, rtg_orient orient) {
     uint64_t m = g->m_input;

@@ -5,6 +5,7 @@
 
 #include <cstdint>
 #include <cstdio>
+#include <set>
 #include <string>
 #include <vector>
 
@@ -27,14 +28,33 @@ struct DeviceBuffer {
 };
 
 // One oriented or symmetric CSR resident in HBM.
+// Bytes of tail padding after every adjacency array: the bulk-copy stager widens a list's
+// byte range to 16-byte boundaries and may read up to 12 bytes past the last element.
+constexpr size_t kAdjPadBytes = 64;
+
 struct Csr {
     uint64_t *off = nullptr;  // n+1
-    uint32_t *adj = nullptr;  // m
+    uint32_t *adj = nullptr;  // m (+ kAdjPadBytes)
     uint32_t *src = nullptr;  // m, source vertex of each entry (oriented CSR only)
     uint32_t n = 0;
     uint64_t m = 0;
     uint32_t max_deg = 0;
     uint64_t work_elems = 0;  // sum over entries (u,v) of deg(u)+deg(v)
+    bool built = false;
+};
+
+// The counting form of an oriented graph: vertices relabelled by rank in (degree, id)
+// order and every edge oriented from the lower rank to the higher one, rows ascending.
+// For an in-edge u->v at position e of N+(u), only the suffix N+(u)[after v] can meet
+// N+(v) (both hold ranks above v), so the in-edge is stored as that element range.
+struct CountCsr {
+    uint64_t *off = nullptr;     // n+1
+    uint32_t *adj = nullptr;     // m (+ kAdjPadBytes), rank ids
+    uint64_t *in_off = nullptr;  // n+1, in-edges grouped by head v
+    uint2 *in_rng = nullptr;     // m: [x, y) = element range of N+(u) after v, per in-edge
+    uint32_t n = 0;
+    uint64_t m = 0;
+    uint32_t max_deg = 0;
     bool built = false;
 };
 
@@ -58,6 +78,9 @@ struct rtg_ctx {
     cudaEvent_t ev[8] = {};
     // grow-only scratch for CUB temp storage and per-call buffers
     rtg::DeviceBuffer scratch[6];
+    // graphs and set collections created on this context (released by rtg_destroy)
+    std::set<rtg_graph *> graphs;
+    std::set<rtg_sets *> sets;
 };
 
 struct rtg_graph {
@@ -67,6 +90,7 @@ struct rtg_graph {
     uint64_t m_input = 0;
     bool edges_released = false;
     rtg::Csr ori;               // oriented CSR
+    rtg::CountCsr cnt;          // rank-relabelled counting form of ori
     int orient = -1;
     rtg::Csr sym;               // symmetric CSR
     rtg::TcPlan *plan_batched = nullptr;
@@ -109,7 +133,10 @@ rtg_status check_status_word(rtg_ctx *ctx);
 
 // CSR builder (csr.cu)
 rtg_status build_csr(rtg_ctx *ctx, rtg_graph *g, rtg_orient orient);
+// counting form (rank relabel + in-edge suffix ranges) of an oriented CSR
+rtg_status csr_build_count(rtg_ctx *ctx, const Csr &c, CountCsr &cc);
 rtg_status graph_free_csr(Csr &c);
+void count_csr_free(CountCsr &cc);
 
 // Triangle counting (tc.cu)
 rtg_status tc_count(rtg_ctx *ctx, rtg_graph *g, rtg_tc_mode mode, uint64_t *total,

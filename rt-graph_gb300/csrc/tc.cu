@@ -8,26 +8,36 @@
 // PLAIN   : classify edges into (family, size) buckets, copy the bucket sizes to the host,
 //           scatter edge ids per bucket, then one grid-stride launch per bucket with one warp
 //           per edge (merge family for balanced pairs, search family for skewed ones).
-// BATCHED : work items (u, first edge) of up to E out-edges of one source vertex, built on
-//           the device; one persistent kernel whose warps take items from an atomic queue,
-//           hash N+(u) once into the warp's shared-memory table and stream every N+(v)
-//           through it. The item build and the count are captured once in a CUDA graph and
-//           replayed. uint64 totals: lane partials -> warp shuffle sum -> block sum -> one
-//           atomicAdd per block.
+// BATCHED : runs on the counting form of the graph (vertices relabelled by (degree, id)
+//           rank, edges low rank -> high rank, rows ascending). For an in-edge u->v only the
+//           suffix of N+(u) after v can meet N+(v), so each in-edge is a ready-made element
+//           range. A work item is (v, first in-edge): up to E in-edges of one vertex v; the
+//           block hashes N+(v) once into a shared-memory table (load <= 1/4) and its warps
+//           take batches of the item's in-edges and stream their suffixes through the table.
+//           Suffixes are staged into a per-warp ring of shared-memory slots by 1-D bulk copies
+//           (cp.async.bulk completing on one mbarrier per slot), so every warp keeps several
+//           lists in flight while it probes the oldest; each lane walks its own elements one
+//           probe step per round, so one long probe chain does not hold the warp.
+//           Streamed elements: sum over u of d+(u)(d+(u)-1)/2, about a quarter of the
+//           push-order work on power-law graphs. Item build + count are one CUDA graph,
+//           captured once per (graph, schedule) and replayed. uint64 totals: lane partials ->
+//           warp shuffle sum -> block sum -> one atomicAdd per block.
 #include <cub/cub.cuh>
 
 #include <algorithm>
 
 #include "internal.h"
 #include "intersect.cuh"
+#include "tma.cuh"
 
 namespace rtg {
 
 namespace {
 
-constexpr uint32_t kDefaultItemEdges = 64;
-constexpr uint32_t kDefaultHashSlots = 2048;
+constexpr uint32_t kDefaultItemEdges = 512;
 constexpr uint32_t kDefaultBlockWarps = 8;
+constexpr uint32_t kDefaultStageSlots = 4;
+constexpr uint32_t kDefaultStageBytes = 1024;
 constexpr uint32_t kPlainRatio = 16;    // long/short above this -> search family (PLAIN)
 constexpr int kPlainBuckets = 6;         // 2 families x 3 size classes
 
@@ -113,78 +123,239 @@ __global__ void __launch_bounds__(256) k_plain_edges(const uint64_t *__restrict_
 
 // ---------------------------------------------------------------- BATCHED form
 
-__global__ void k_item_counts(const uint64_t *__restrict__ off, uint32_t n, uint32_t E,
+// items per vertex v: ceil(indeg(v) / E) when v has out-neighbours and in-neighbours
+__global__ void k_item_counts(const uint64_t *__restrict__ off,
+                              const uint64_t *__restrict__ in_off, uint32_t n, uint32_t E,
                               uint32_t *cnt) {
-    for (uint64_t u = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; u <= n;
-         u += (uint64_t)gridDim.x * blockDim.x) {
+    for (uint64_t v = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; v <= n;
+         v += (uint64_t)gridDim.x * blockDim.x) {
         uint32_t c = 0;
-        if (u < n) {
-            uint32_t a = (uint32_t)(off[u + 1] - off[u]);
-            c = (a >= 2) ? (a + E - 1) / E : 0u;
+        if (v < n) {
+            uint32_t b = (uint32_t)(off[v + 1] - off[v]);
+            uint32_t indeg = (uint32_t)(in_off[v + 1] - in_off[v]);
+            c = (b >= 1 && indeg >= 1) ? (indeg + E - 1) / E : 0u;
         }
-        cnt[u] = c;
+        cnt[v] = c;
     }
 }
 
-__global__ void k_item_fill(const uint64_t *__restrict__ off, uint32_t n, uint32_t E,
-                            const uint32_t *__restrict__ base, uint64_t *items,
-                            unsigned long long *acc) {
-    for (uint64_t u = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; u < n;
-         u += (uint64_t)gridDim.x * blockDim.x) {
-        uint32_t a = (uint32_t)(off[u + 1] - off[u]);
-        if (a < 2) continue;
-        uint32_t b0 = base[u];
+__global__ void k_item_fill(const uint64_t *__restrict__ off, const uint64_t *__restrict__ in_off,
+                            uint32_t n, uint32_t E, const uint32_t *__restrict__ base,
+                            uint64_t *items, unsigned long long *acc) {
+    for (uint64_t v = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; v < n;
+         v += (uint64_t)gridDim.x * blockDim.x) {
+        uint32_t b = (uint32_t)(off[v + 1] - off[v]);
+        uint32_t indeg = (uint32_t)(in_off[v + 1] - in_off[v]);
+        if (b < 1 || indeg < 1) continue;
+        uint32_t b0 = base[v];
         uint32_t k = 0;
-        for (uint32_t j = 0; j < a; j += E, ++k) items[b0 + k] = (u << 32) | j;
+        for (uint32_t j = 0; j < indeg; j += E, ++k) items[b0 + k] = (v << 32) | j;
     }
     if (blockIdx.x == 0 && threadIdx.x == 0) acc[2] = base[n];
 }
 
-// acc[0] = total, acc[1] = queue head, acc[2] = number of items
-__global__ void k_tc_batched(const uint64_t *__restrict__ off, const uint32_t *__restrict__ adj,
-                             const uint64_t *__restrict__ items, unsigned long long *acc,
-                             uint32_t E, uint32_t H) {
-    extern __shared__ __align__(16) uint32_t smem[];
+struct BlkCfg {
+    uint32_t E;           // in-edges per block item
+    uint32_t T;           // hash-table slots per block
+    uint32_t S;           // staging slots per warp
+    uint32_t slot_bytes;  // bytes per staging slot
+    uint32_t meta_off;    // byte offsets of the shared-memory regions
+    uint32_t tab_off;
+    uint32_t ring_off;
+};
+
+constexpr uint32_t kBatch = 32;  // in-edges a warp takes from its block's item at a time
+
+// table size for a list of b elements: 4b slots rounded up to a power of two (load <= 1/4)
+// within [32, T]; b <= T/2 keeps the load at or below 1/2.
+__device__ __forceinline__ uint32_t table_lg(uint32_t b, uint32_t T) {
+    uint32_t lg = 5;
+    while ((1u << lg) < 4 * b && (1u << lg) < T) ++lg;
+    return lg;
+}
+
+// acc[0] = total, acc[1] = item queue head, acc[2] = number of items
+__global__ void k_tc_block(const uint64_t *__restrict__ off, const uint32_t *__restrict__ adj,
+                           const uint64_t *__restrict__ in_off, const uint2 *__restrict__ in_rng,
+                           const uint64_t *__restrict__ items, unsigned long long *acc, BlkCfg p,
+                           uint32_t *status) {
+    extern __shared__ __align__(128) unsigned char smem[];
     __shared__ unsigned long long red[32];
+    __shared__ uint32_t s_v, s_k0, s_next, s_stop;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    uint32_t *tab = smem + warp * H;
+    uint32_t *tab = reinterpret_cast<uint32_t *>(smem + p.tab_off);
+    uint64_t *bars = reinterpret_cast<uint64_t *>(smem) + (size_t)warp * p.S;
+    uint32_t *meta = reinterpret_cast<uint32_t *>(smem + p.meta_off) + (size_t)warp * p.S * 2;
+    unsigned char *ring = smem + p.ring_off + (size_t)warp * p.S * p.slot_bytes;
+    if ((uint32_t)lane < p.S) mbar_init(bars + lane, 1);
+    fence_mbar_init();
+    if (threadIdx.x == 0) s_stop = 0;
+    __syncthreads();
+    const uint32_t CH = p.slot_bytes / 4 - 4;  // list elements per staged chunk
     const unsigned long long nitems = acc[2];
+    uint32_t phase = 0;                        // parity bit per staging slot
     unsigned long long cnt = 0;
+
     while (true) {
-        unsigned long long k = 0;
-        if (lane == 0) k = atomicAdd(&acc[1], 1ull);
-        k = __shfl_sync(kFull, k, 0);
-        if (k >= nitems) break;
-        const uint64_t it = items[k];
-        const uint32_t u = (uint32_t)(it >> 32), j0 = (uint32_t)it;
-        const uint64_t ou = off[u];
-        const uint32_t a = (uint32_t)(off[u + 1] - ou);
-        const uint32_t j1 = min(j0 + E, a);
-        const uint32_t *Nu = adj + ou;
-        const bool hashed = a <= H / 2;
-        uint32_t lg = 0;
-        if (hashed) {
-            lg = hash_lg_for(a);
-            warp_hash_build(tab, lg, Nu, a, lane);
-        }
-        for (uint32_t jb = j0; jb < j1; jb += 32) {
-            // the next (up to) 32 out-neighbours v and their list bounds, one per lane
-            const uint32_t j = jb + lane;
-            const bool ok = j < j1;
-            const uint32_t v = ok ? __ldg(Nu + j) : 0u;
-            const uint64_t ov = ok ? __ldg(off + v) : 0ull;
-            const uint32_t bl = ok ? (uint32_t)(__ldg(off + v + 1) - ov) : 0u;
-            const uint32_t ne = min(32u, j1 - jb);
-            for (uint32_t e = 0; e < ne; ++e) {
-                const uint64_t ove = __shfl_sync(kFull, ov, e);
-                const uint32_t be = __shfl_sync(kFull, bl, e);
-                if (be == 0) continue;
-                const uint32_t *Nv = adj + ove;
-                if (hashed) cnt += warp_hash_stream(tab, lg, Nv, be, lane);
-                else cnt += warp_merge_count(Nu, a, Nv, be, lane);
+        if (threadIdx.x == 0) {
+            const unsigned long long k = s_stop ? nitems : atomicAdd(&acc[1], 1ull);
+            if (k >= nitems) {
+                s_v = kEmpty;
+            } else {
+                const uint64_t it = items[k];
+                s_v = (uint32_t)(it >> 32);
+                s_k0 = (uint32_t)it;
+                s_next = (uint32_t)it;
             }
         }
-        __syncwarp();
+        __syncthreads();
+        const uint32_t v = s_v;
+        if (v == kEmpty) break;
+        const uint64_t ov = off[v];
+        const uint32_t b = (uint32_t)(off[v + 1] - ov);
+        const uint64_t kin = in_off[v];
+        const uint32_t k1 = min(s_k0 + p.E, (uint32_t)(in_off[v + 1] - kin));
+        const uint32_t *Nv = adj + ov;
+        const bool hashed = b <= p.T / 2;
+        uint32_t lg = 0, mask = 0;
+        if (hashed) {
+            lg = table_lg(b, p.T);
+            mask = (1u << lg) - 1;
+            uint4 *t4 = reinterpret_cast<uint4 *>(tab);
+            const uint4 e4 = make_uint4(kEmpty, kEmpty, kEmpty, kEmpty);
+            for (uint32_t q = threadIdx.x; q < (1u << lg) / 4; q += blockDim.x) t4[q] = e4;
+            __syncthreads();
+            for (uint32_t q = threadIdx.x; q < b; q += blockDim.x) {
+                const uint32_t w = __ldg(Nv + q);
+                uint32_t sl = hash_slot(w, lg);
+                while (atomicCAS(&tab[sl], kEmpty, w) != kEmpty) sl = (sl + 1) & mask;
+            }
+            __syncthreads();
+        }
+
+        if (!hashed) {
+            // N+(v) too long for the table: tile merge of every suffix with N+(v)
+            while (true) {
+                uint32_t kb = 0;
+                if (lane == 0) kb = atomicAdd(&s_next, 1u);
+                kb = __shfl_sync(kFull, kb, 0);
+                if (kb >= k1) break;
+                const uint2 r = in_rng[kin + kb];
+                cnt += warp_merge_count(adj + r.x, r.y - r.x, Nv, b, lane);
+            }
+        } else {
+            // batches of in-edges: lane i holds the suffix range of edge kb + i; the next
+            // batch is taken and its ranges loaded while the current one is staged
+            auto take_batch = [&](uint32_t &kb, uint32_t &nb, uint2 &r) {
+                uint32_t x = 0;
+                if (lane == 0) x = atomicAdd(&s_next, kBatch);
+                kb = __shfl_sync(kFull, x, 0);
+                nb = kb < k1 ? min(kBatch, k1 - kb) : 0u;
+                r = ((uint32_t)lane < nb) ? __ldg(in_rng + kin + kb + lane) : make_uint2(0u, 0u);
+            };
+            uint32_t kb, nb, nkb, nnb;
+            uint2 my_r, nx_r;
+            take_batch(kb, nb, my_r);
+            take_batch(nkb, nnb, nx_r);
+            uint32_t e = 0;
+            uint32_t ex = __shfl_sync(kFull, my_r.x, 0), ey = __shfl_sync(kFull, my_r.y, 0);
+            bool done = nb == 0;
+            uint32_t inflight = 0, sw = 0, sr = 0;
+            bool failed = false;
+            while (true) {
+                while (inflight < p.S && !done) {
+                    uint32_t start = 0, len = 0;
+                    while (true) {
+                        if (e >= nb) {
+                            if (nnb == 0) {
+                                done = true;
+                                break;
+                            }
+                            kb = nkb;
+                            nb = nnb;
+                            my_r = nx_r;
+                            take_batch(nkb, nnb, nx_r);
+                            e = 0;
+                            ex = __shfl_sync(kFull, my_r.x, 0);
+                            ey = __shfl_sync(kFull, my_r.y, 0);
+                            continue;
+                        }
+                        if (ex < ey) {
+                            start = ex;
+                            len = min(CH, ey - ex);
+                            ex += len;
+                            break;
+                        }
+                        ++e;
+                        const uint32_t ee = e < nb ? e : 0u;
+                        ex = __shfl_sync(kFull, my_r.x, ee);
+                        ey = __shfl_sync(kFull, my_r.y, ee);
+                    }
+                    if (done) break;
+                    const uintptr_t ga = reinterpret_cast<uintptr_t>(adj + start);
+                    const uintptr_t gb = ga & ~(uintptr_t)15;
+                    const uint32_t head = (uint32_t)(ga - gb) >> 2;
+                    const uint32_t bytes = ((head + len) * 4u + 15u) & ~15u;
+                    if (lane == 0) {
+                        meta[2 * sw] = head;
+                        meta[2 * sw + 1] = len;
+                        mbar_arrive_expect_tx(bars + sw, bytes);
+                        bulk_copy_g2s(ring + (size_t)sw * p.slot_bytes,
+                                      reinterpret_cast<const void *>(gb), bytes, bars + sw);
+                    }
+                    sw = (sw + 1 == p.S) ? 0 : sw + 1;
+                    ++inflight;
+                }
+                if (inflight == 0) break;
+                __syncwarp();
+                if (!mbar_wait(bars + sr, (phase >> sr) & 1u)) {
+                    if (lane == 0) {
+                        atomicExch(status, kStatusTimeout);
+                        atomicExch(&s_stop, 1u);
+                    }
+                    for (uint32_t q = 1; q < inflight; ++q) {  // bounded drain of the others
+                        const uint32_t s2 = (sr + q) % p.S;
+                        mbar_wait(bars + s2, (phase >> s2) & 1u);
+                    }
+                    failed = true;
+                    break;
+                }
+                phase ^= 1u << sr;
+                const uint32_t head = meta[2 * sr], len = meta[2 * sr + 1];
+                const uint32_t *data =
+                    reinterpret_cast<const uint32_t *>(ring + (size_t)sr * p.slot_bytes) + head;
+                // every lane walks its own elements (t = lane, lane+32, ...) one probe step per
+                // round, so a long probe chain on one lane does not hold the others
+                uint32_t t = lane;
+                bool act = t < len;
+                uint32_t w = act ? data[t] : 0u;
+                uint32_t sl = act ? hash_slot(w, lg) : 0u;
+                while (__any_sync(kFull, act)) {
+                    if (act) {
+                        const uint32_t x = tab[sl];
+                        if (x == w || x == kEmpty) {
+                            cnt += (x == w);
+                            t += 32;
+                            act = t < len;
+                            if (act) {
+                                w = data[t];
+                                sl = hash_slot(w, lg);
+                            }
+                        } else {
+                            sl = (sl + 1) & mask;
+                        }
+                    }
+                }
+                __syncwarp();
+                fence_proxy_async_smem();
+                sr = (sr + 1 == p.S) ? 0 : sr + 1;
+                --inflight;
+            }
+            if (failed) {
+                // leave this item; s_stop ends the block after it
+            }
+        }
+        __syncthreads();  // the table is rebuilt for the next item
     }
     block_add_total(cnt, &acc[0], red);
 }
@@ -231,15 +402,19 @@ namespace {
 rtg_config effective_config(const rtg_ctx *ctx) {
     rtg_config c = ctx->cfg;
     if (!c.tc_item_edges) c.tc_item_edges = kDefaultItemEdges;
-    if (!c.tc_hash_slots) c.tc_hash_slots = kDefaultHashSlots;
     if (!c.tc_block_warps) c.tc_block_warps = kDefaultBlockWarps;
+    if (!c.tc_stage_slots) c.tc_stage_slots = kDefaultStageSlots;
+    if (!c.tc_stage_bytes) c.tc_stage_bytes = kDefaultStageBytes;
     return c;
 }
 
 bool same_tc_config(const rtg_config &a, const rtg_config &b) {
     return a.tc_item_edges == b.tc_item_edges && a.tc_hash_slots == b.tc_hash_slots &&
-           a.tc_block_warps == b.tc_block_warps && a.tc_blocks_per_sm == b.tc_blocks_per_sm;
+           a.tc_block_warps == b.tc_block_warps && a.tc_blocks_per_sm == b.tc_blocks_per_sm &&
+           a.tc_stage_slots == b.tc_stage_slots && a.tc_stage_bytes == b.tc_stage_bytes;
 }
+
+inline uint32_t align128(uint32_t x) { return (x + 127u) & ~127u; }
 
 rtg_status batched_plan(rtg_ctx *ctx, rtg_graph *g, TcPlan **out) {
     rtg_config cfg = effective_config(ctx);
@@ -256,8 +431,28 @@ rtg_status batched_plan(rtg_ctx *ctx, rtg_graph *g, TcPlan **out) {
         tc_plan_free(p);
         return s;
     };
-    const Csr &c = g->ori;
-    const uint32_t E = cfg.tc_item_edges, H = cfg.tc_hash_slots, W = cfg.tc_block_warps;
+    const CountCsr &c = g->cnt;
+    if (!c.built)
+        return bail(fail(ctx, RTG_ERR_STATE, "counting form of the CSR is missing"));
+    const uint32_t E = cfg.tc_item_edges, W = cfg.tc_block_warps;
+    BlkCfg pc{};
+    pc.E = E;
+    // table: explicit size, else 4x the longest out-list (power of two) in [1024, 16384]
+    uint32_t T = cfg.tc_hash_slots;
+    if (!T) {
+        T = 1024;
+        while (T < 4ull * c.max_deg && T < 16384) T <<= 1;
+    }
+    pc.T = T;
+    pc.S = cfg.tc_stage_slots;
+    pc.slot_bytes = cfg.tc_stage_bytes;
+    pc.meta_off = W * pc.S * 8;
+    pc.tab_off = align128(pc.meta_off + W * pc.S * 8);
+    pc.ring_off = align128(pc.tab_off + pc.T * 4);
+    const size_t smem = (size_t)pc.ring_off + (size_t)W * pc.S * pc.slot_bytes;
+    if (smem + 256 > (size_t)ctx->smem_optin)
+        return bail(fail(ctx, RTG_ERR_INVALID_ARG, "schedule needs %zu B of shared memory", smem));
+
     const uint64_t item_cap = c.m / E + c.n + 1;
     rtg_status s;
     if ((s = dev_alloc(ctx, (void **)&p->items, item_cap * 8)) != RTG_OK) return bail(s);
@@ -273,16 +468,12 @@ rtg_status batched_plan(rtg_ctx *ctx, rtg_graph *g, TcPlan **out) {
     if ((e = cudaEventCreate(&p->k0)) != cudaSuccess ||
         (e = cudaEventCreate(&p->k1)) != cudaSuccess)
         return bail(cuda_fail(ctx, e, "event", __FILE__, __LINE__));
-
-    const size_t smem = (size_t)W * H * 4;
-    if ((int)smem > ctx->smem_optin)
-        return bail(fail(ctx, RTG_ERR_INVALID_ARG, "schedule needs %zu B of shared memory", smem));
-    if ((e = cudaFuncSetAttribute(k_tc_batched, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    if ((e = cudaFuncSetAttribute(k_tc_block, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                   (int)smem)) != cudaSuccess)
         return bail(cuda_fail(ctx, e, "smem attribute", __FILE__, __LINE__));
     int per_sm = 0;
-    if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_tc_batched, W * 32,
-                                                           smem)) != cudaSuccess)
+    if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_tc_block, W * 32, smem)) !=
+        cudaSuccess)
         return bail(cuda_fail(ctx, e, "occupancy", __FILE__, __LINE__));
     if (cfg.tc_blocks_per_sm) per_sm = std::min<int>(per_sm, (int)cfg.tc_blocks_per_sm);
     per_sm = std::max(per_sm, 1);
@@ -295,12 +486,13 @@ rtg_status batched_plan(rtg_ctx *ctx, rtg_graph *g, TcPlan **out) {
         cudaSuccess)
         return bail(cuda_fail(ctx, e, "capture", __FILE__, __LINE__));
     cudaMemsetAsync(p->acc, 0, 8 * sizeof(unsigned long long), ctx->stream);
-    k_item_counts<<<g1, 256, 0, ctx->stream>>>(c.off, c.n, E, p->vcnt);
+    k_item_counts<<<g1, 256, 0, ctx->stream>>>(c.off, c.in_off, c.n, E, p->vcnt);
     cub::DeviceScan::ExclusiveSum(p->cub_tmp, cub_bytes, p->vcnt, vbase, (int64_t)c.n + 1,
                                   ctx->stream);
-    k_item_fill<<<g1, 256, 0, ctx->stream>>>(c.off, c.n, E, vbase, p->items, p->acc);
+    k_item_fill<<<g1, 256, 0, ctx->stream>>>(c.off, c.in_off, c.n, E, vbase, p->items, p->acc);
     cudaEventRecordWithFlags(p->k0, ctx->stream, cudaEventRecordExternal);
-    k_tc_batched<<<grid, W * 32, smem, ctx->stream>>>(c.off, c.adj, p->items, p->acc, E, H);
+    k_tc_block<<<grid, W * 32, smem, ctx->stream>>>(c.off, c.adj, c.in_off, c.in_rng, p->items,
+                                                    p->acc, pc, ctx->d_status);
     cudaEventRecordWithFlags(p->k1, ctx->stream, cudaEventRecordExternal);
     e = cudaStreamEndCapture(ctx->stream, &p->graph);
     if (e != cudaSuccess) return bail(cuda_fail(ctx, e, "end capture", __FILE__, __LINE__));
@@ -331,6 +523,7 @@ rtg_status count_batched(rtg_ctx *ctx, rtg_graph *g, uint64_t *total, rtg_timing
     RTG_CUDA(ctx, cudaMemcpyAsync(&h, p->acc, 8, cudaMemcpyDeviceToHost, ctx->stream));
     RTG_CUDA(ctx, cudaEventRecord(ctx->ev[2], ctx->stream));
     RTG_CUDA(ctx, cudaEventSynchronize(ctx->ev[2]));
+    RTG_TRY(check_status_word(ctx));
     *total = h;
     float ms = 0, kms = 0, dms = 0;
     cudaEventElapsedTime(&ms, ctx->ev[0], ctx->ev[1]);

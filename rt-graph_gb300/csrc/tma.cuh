@@ -1,0 +1,73 @@
+// Inline-PTX helpers for the bulk-copy (TMA) staging pipeline: 1-D cp.async.bulk
+// global -> shared copies completing on shared-memory mbarriers.
+//
+// Rules kept by every caller:
+//  * source and destination addresses are 16-byte aligned and the size is a multiple of
+//    16 bytes (the source range is widened to 16-byte boundaries; device arrays that are
+//    staged this way are allocated with 16 bytes of tail padding);
+//  * no cluster multicast; the copy lands in the issuing CTA's own shared memory;
+//  * every wait is bounded: mbar_wait() gives up after kMaxWaitIters polls and reports
+//    failure, and the caller records a status word instead of spinning forever.
+#pragma once
+
+#include <cstdint>
+
+namespace rtg {
+
+constexpr uint32_t kMaxWaitIters = 1u << 22;
+
+__device__ __forceinline__ uint32_t smem_u32(const void *p) {
+    return (uint32_t)__cvta_generic_to_shared(p);
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count)
+                 : "memory");
+}
+
+// make mbarrier initialisation visible to the async (bulk-copy) proxy
+__device__ __forceinline__ void fence_mbar_init() {
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+
+// order this thread's earlier generic-proxy shared-memory accesses before later
+// async-proxy writes into the same buffer
+__device__ __forceinline__ void fence_proxy_async_smem() {
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t *bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)),
+                 "r"(bytes)
+                 : "memory");
+}
+
+__device__ __forceinline__ void bulk_copy_g2s(void *dst, const void *src, uint32_t bytes,
+                                              uint64_t *bar) {
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::
+            "r"(smem_u32(dst)),
+        "l"((uint64_t)__cvta_generic_to_global(src)), "r"(bytes), "r"(smem_u32(bar))
+        : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(smem_u32(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+
+// Wait for the phase with the given parity to complete; false after kMaxWaitIters polls.
+__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity) {
+    for (uint32_t it = 0; it < kMaxWaitIters; ++it)
+        if (mbar_try_wait(bar, parity)) return true;
+    return false;
+}
+
+}  // namespace rtg

@@ -8,6 +8,7 @@ from __future__ import annotations
 
 import ctypes as C
 import os
+import weakref
 from pathlib import Path
 
 import numpy as np
@@ -51,6 +52,7 @@ class GraphInfo(C.Structure):
 class Config(C.Structure):
     _fields_ = [(k, C.c_uint32) for k in (
         "tc_block_warps", "tc_item_edges", "tc_hash_slots", "tc_blocks_per_sm",
+        "tc_stage_slots", "tc_stage_bytes",
         "si_block_warps", "si_search_ratio", "si_split_len", "si_pairs_per_grab")]
 
     def as_dict(self) -> dict:
@@ -244,12 +246,15 @@ def device_available() -> bool:
 class Context:
     def __init__(self, device: int = 0):
         self.h = P()
+        self.children = weakref.WeakSet()   # graphs / set collections made on this context
         st = lib.rtg_init(device, C.byref(self.h))
         if st != OK:
             raise RtgError(st, f"rtg_init(device={device}) failed")
 
     def close(self) -> None:
         if self.h:
+            for ch in list(self.children):
+                ch.close()
             lib.rtg_destroy(self.h)
             self.h = P()
 
@@ -379,10 +384,12 @@ class Graph:
     def __init__(self, ctx: Context, h):
         self.ctx = ctx
         self.h = h
+        ctx.children.add(self)
 
     def close(self) -> None:
         if self.h:
-            lib.rtg_graph_destroy(self.h)
+            if self.ctx.h:   # a closed context has already released its graphs
+                lib.rtg_graph_destroy(self.h)
             self.h = P()
 
     def __del__(self):
@@ -436,10 +443,12 @@ class Sets:
     def __init__(self, ctx: Context, h):
         self.ctx = ctx
         self.h = h
+        ctx.children.add(self)
 
     def close(self) -> None:
         if self.h:
-            lib.rtg_sets_destroy(self.h)
+            if self.ctx.h:   # a closed context has already released its set collections
+                lib.rtg_sets_destroy(self.h)
             self.h = P()
 
     def __del__(self):

@@ -1,0 +1,205 @@
+"""Triangle-counting parity on the GPU, through the C ABI.
+
+Bit-exact against the reference-produced golden vectors (CSR and count) and against the
+oracle; at full configuration sizes through the oracle merge counter and structural
+properties of the GPU-built CSR.
+"""
+from __future__ import annotations
+
+from math import comb
+
+import numpy as np
+import pytest
+
+import oracle
+import rtg
+from conftest import golden_edges, sha_i32, tc_golden
+
+pytestmark = pytest.mark.gpu
+TC = tc_golden()
+MODES = (rtg.TC_PLAIN, rtg.TC_BATCHED)
+
+
+@pytest.mark.parametrize("name", sorted(TC))
+def test_reference_mode_csr_and_count_bit_exact(ctx, name):
+    rec = TC[name]
+    s, d = golden_edges(rec)
+    g = ctx.graph_from_edges(s, d).build(rtg.ORIENT_DEGREE_RAW_REF)
+    info = g.info()
+    assert (info.n, info.m) == (rec["nodes"], rec["edges"])
+    off, adj = g.csr()
+    assert sha_i32(off) == rec["offsets_sha256"]
+    assert sha_i32(adj) == rec["adjs_sha256"]
+    for mode in MODES:
+        assert g.tc(mode)[0] == rec["triangles"]
+
+
+@pytest.mark.parametrize("name", sorted(TC))
+def test_degree_mode_csr_matches_oracle(ctx, name):
+    rec = TC[name]
+    s, d = golden_edges(rec)
+    g = ctx.graph_from_edges(s, d).build(rtg.ORIENT_DEGREE)
+    off, adj = g.csr()
+    ooff, oadj = oracle.degree_csr(s, d)
+    assert np.array_equal(off, ooff)
+    assert np.array_equal(adj, oadj)
+    for mode in MODES:
+        assert g.tc(mode)[0] == rec["triangles"]
+
+
+@pytest.mark.parametrize("name", sorted(TC))
+def test_symmetric_csr_matches_oracle(ctx, name):
+    s, d = golden_edges(TC[name])
+    g = ctx.graph_from_edges(s, d).build(rtg.ORIENT_SYMMETRIC)
+    off, adj = g.csr(symmetric=True)
+    ooff, oadj = oracle.symmetric_csr(s, d)
+    assert np.array_equal(off, ooff)
+    assert np.array_equal(adj, oadj)
+
+
+def test_empty_and_tiny(ctx):
+    for s, d in [([], []), ([0], [1]), ([3], [3]), ([0, 1], [1, 0])]:
+        s = np.array(s, np.uint32)
+        d = np.array(d, np.uint32)
+        for orient in (rtg.ORIENT_DEGREE, rtg.ORIENT_DEGREE_RAW_REF):
+            g = ctx.graph_from_edges(s, d).build(orient)
+            for mode in MODES:
+                assert g.tc(mode)[0] == 0
+
+
+@pytest.mark.parametrize("n", [3, 4, 33, 65, 200])
+def test_cliques_closed_form(ctx, n):
+    s, d = zip(*[(i, j) for i in range(n) for j in range(i + 1, n)])
+    g = ctx.graph_from_edges(np.array(s), np.array(d)).build(rtg.ORIENT_DEGREE)
+    for mode in MODES:
+        assert g.tc(mode)[0] == comb(n, 3)
+
+
+@pytest.mark.parametrize("cfg", [
+    dict(tc_item_edges=1), dict(tc_item_edges=7), dict(tc_item_edges=1024),
+    dict(tc_hash_slots=64), dict(tc_hash_slots=256), dict(tc_hash_slots=8192, tc_block_warps=4),
+    dict(tc_block_warps=1),
+    dict(tc_block_warps=16, tc_hash_slots=1024, tc_stage_slots=2, tc_stage_bytes=1024),
+    dict(tc_blocks_per_sm=1),
+    dict(tc_stage_slots=2), dict(tc_stage_slots=16, tc_block_warps=2),
+    dict(tc_stage_bytes=256), dict(tc_stage_bytes=256, tc_stage_slots=3, tc_item_edges=5),
+    dict(tc_stage_bytes=8192, tc_stage_slots=4, tc_block_warps=2),
+])
+def test_batched_schedules_agree(ctx, cfg):
+    old = ctx.config()
+    try:
+        ctx.set_config(**cfg)
+        for name in ("rmat_s14_ef16_s42", "hk_n20000_m6_p0.9_s3", "rmat_s10_ef8_s5_skewed"):
+            rec = TC[name]
+            s, d = golden_edges(rec)
+            g = ctx.graph_from_edges(s, d).build(rtg.ORIENT_DEGREE)
+            assert g.tc(rtg.TC_BATCHED)[0] == rec["triangles"], (name, cfg)
+    finally:
+        ctx.set_config(**old.as_dict())
+
+
+def test_hub_heavy_graph_uses_merge_fallback(ctx):
+    # a dense core makes out-degrees exceed the per-warp hash capacity
+    rng = np.random.default_rng(3)
+    n = 3000
+    s, d = np.triu_indices(n, 1)
+    keep = rng.random(len(s)) < 0.5
+    s, d = s[keep].astype(np.uint32), d[keep].astype(np.uint32)
+    off, adj = oracle.degree_csr(s, d)
+    want = oracle.tc_merge(off, adj)
+    g = ctx.graph_from_edges(s, d).build(rtg.ORIENT_DEGREE)
+    assert g.info().max_out_degree > 1024
+    for mode in MODES:
+        assert g.tc(mode)[0] == want
+
+
+def test_repeatable(ctx):
+    s, d = golden_edges(TC["rmat_s14_ef16_s42"])
+    g = ctx.graph_from_edges(s, d).build(rtg.ORIENT_DEGREE)
+    got = {g.tc(rtg.TC_BATCHED)[0] for _ in range(10)} | {g.tc(rtg.TC_PLAIN)[0] for _ in range(3)}
+    assert got == {TC["rmat_s14_ef16_s42"]["triangles"]}
+
+
+def test_drop_in_host_csr_and_host_edges(ctx):
+    for name in ("k4_noise", "ba_n4096_m4_s7", "rmat_s12_ef16_s1"):
+        rec = TC[name]
+        s, d = golden_edges(rec)
+        pairs = np.stack([s.astype(np.int32), d.astype(np.int32)], axis=1)
+        _, _, off, adj = oracle.reference_csr(pairs)
+        for mode in MODES:
+            got, t = ctx.tc_count_host_csr(off, adj, mode)
+            assert got == rec["triangles"]
+            got, t = ctx.tc_count_host_edges(s, d, rtg.ORIENT_DEGREE_RAW_REF, mode)
+            assert got == rec["triangles"]
+            assert t.h2d_bytes == 8 * len(s) and t.kernel_launches > 0
+
+
+def test_file_formats(ctx, tmp_path):
+    rec = TC["wheel"]
+    s, d = golden_edges(rec)
+    rtg.edges_write_bin(str(tmp_path / "g.edge"), s, d)
+    (tmp_path / "g.txt").write_text("# comment\n" + "".join(f"{a} {b}\n" for a, b in zip(s, d)))
+    lines = ["%%MatrixMarket matrix coordinate pattern symmetric", "% c",
+             f"{int(max(s.max(), d.max())) + 1} {int(max(s.max(), d.max())) + 1} {len(s)}"]
+    lines += [f"{a + 1} {b + 1}" for a, b in zip(s, d)]
+    (tmp_path / "g.mtx").write_text("\n".join(lines) + "\n")
+    for path, fmt in (("g.edge", rtg.FMT_EDGE_BIN), ("g.txt", rtg.FMT_EDGE_TXT),
+                      ("g.mtx", rtg.FMT_MTX)):
+        g = ctx.graph_load(str(tmp_path / path), fmt).build(rtg.ORIENT_DEGREE)
+        assert g.tc()[0] == rec["triangles"]
+
+
+def test_errors_are_status_codes(ctx):
+    with pytest.raises(rtg.RtgError) as e:
+        ctx.graph_from_edges(np.array([0xFFFFFFFF], np.uint32),
+                             np.array([1], np.uint32)).build(rtg.ORIENT_DEGREE)
+    assert e.value.status == rtg.ERR_INVALID_ARG
+    g = ctx.graph_from_edges(np.array([0, 1], np.uint32), np.array([1, 2], np.uint32))
+    with pytest.raises(rtg.RtgError) as e:
+        g.tc()
+    assert e.value.status == rtg.ERR_STATE
+    with pytest.raises(rtg.RtgError) as e:   # unsorted row
+        ctx.graph_from_csr(np.array([0, 2, 2, 2], np.int32), np.array([2, 1], np.int32))
+    assert e.value.status == rtg.ERR_INVALID_ARG
+    # the context is still usable after errors
+    assert ctx.graph_from_edges(np.array([0, 1, 2], np.uint32),
+                                np.array([1, 2, 0], np.uint32)).build().tc()[0] == 1
+
+
+def test_config2_holme_kim_full_size(ctx):
+    """Holme-Kim n=2^20, m=16, p=0.3 (~16.7M edges): GPU vs oracle merge counter."""
+    s, d = rtg.gen_hk(1 << 20, 16, 0.3, seed=1)
+    g = ctx.graph_from_edges(s, d).build(rtg.ORIENT_DEGREE)
+    off, adj = g.csr()
+    want = oracle.tc_merge(off, adj)
+    assert g.tc(rtg.TC_PLAIN)[0] == want
+    assert g.tc(rtg.TC_BATCHED)[0] == want
+    # the reference-mode CSR gives the same total
+    g2 = ctx.graph_from_edges(s, d).build(rtg.ORIENT_DEGREE_RAW_REF)
+    assert g2.tc(rtg.TC_BATCHED)[0] == want
+
+
+def _check_oriented_csr(off, adj):
+    deg_out = np.diff(off.astype(np.int64))
+    n = len(off) - 1
+    src = np.repeat(np.arange(n, dtype=np.int64), deg_out)
+    # rows strictly ascending
+    same = src[1:] == src[:-1]
+    assert (adj[1:][same] > adj[:-1][same]).all()
+    # no self loops; total degree order respected (an acyclic orientation)
+    assert (src != adj).all()
+    deg = np.bincount(src, minlength=n) + np.bincount(adj, minlength=n)
+    a = deg[src] * (n + 1) + src
+    b = deg[adj] * (n + 1) + adj
+    assert (a < b).all()
+
+
+def test_config4_rmat21_full_size(ctx):
+    """R-MAT scale 21, ef 16: PLAIN == BATCHED == oracle merge count; CSR checked."""
+    s, d = rtg.gen_rmat(21, 16, 0.57, 0.19, 0.19, seed=42)
+    g = ctx.graph_from_edges(s, d).build(rtg.ORIENT_DEGREE)
+    off, adj = g.csr()
+    _check_oriented_csr(off, adj)
+    want = oracle.tc_merge(off, adj)
+    assert g.tc(rtg.TC_BATCHED)[0] == want
+    assert g.tc(rtg.TC_PLAIN)[0] == want
