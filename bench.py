@@ -291,7 +291,7 @@ def run_gpu(args, dist: Dist) -> None:
     achieved = algo_bytes / (kms / 1e3) / 1e9
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",
                 "frac": achieved / peaks["hbm_gbs"], "traffic": profile_traffic("tc_batched_rmat21"),
-                "peak_source": peaks["source"], "kernel": "k_tc_batched",
+                "peak_source": peaks["source"], "kernel": "k_tc_warp",
                 "kernel_ms": kms, "algo_bytes_per_launch": algo_bytes}
     cpu = None
     if dist.rank == 0 and dist.ws == 1 and not args.no_cpu_baseline:

@@ -11,13 +11,14 @@
 // BATCHED : runs on the counting form of the graph (vertices relabelled by (degree, id)
 //           rank, edges low rank -> high rank, rows ascending). For an in-edge u->v only the
 //           suffix of N+(u) after v can meet N+(v), so each in-edge is a ready-made element
-//           range. A work item is (v, first in-edge): up to E in-edges of one vertex v; the
-//           block hashes N+(v) once into a shared-memory table (load <= 1/4) and its warps
-//           take batches of the item's in-edges and stream their suffixes through the table.
-//           Suffixes are staged into a per-warp ring of shared-memory slots by 1-D bulk copies
-//           (cp.async.bulk completing on one mbarrier per slot), so every warp keeps several
-//           lists in flight while it probes the oldest; each lane walks its own elements one
-//           probe step per round, so one long probe chain does not hold the warp.
+//           range. A work item is (v, first in-edge): up to E in-edges of one vertex v, taken
+//           by one warp from a device queue (persistent kernel, no block barriers). The warp
+//           marks N+(v) in its shared-memory region: as a bitmap over the ranks (v, n) when
+//           n - v - 1 fits the region (high-rank v, which carry almost all of the work on
+//           power-law graphs), else as an open-addressing hash table, else (out-list too long
+//           for the table) it falls back to a tile merge. It then streams the suffixes of the
+//           item's in-edges with coalesced loads, one 128-element block loaded ahead of the
+//           block being tested, and tests every element with one shared-memory load.
 //           Streamed elements: sum over u of d+(u)(d+(u)-1)/2, about a quarter of the
 //           push-order work on power-law graphs. Item build + count are one CUDA graph,
 //           captured once per (graph, schedule) and replayed. uint64 totals: lane partials ->
@@ -34,8 +35,9 @@ namespace rtg {
 
 namespace {
 
-constexpr uint32_t kDefaultItemEdges = 512;
+constexpr uint32_t kDefaultItemEdges = 64;
 constexpr uint32_t kDefaultBlockWarps = 8;
+constexpr uint32_t kDefaultRegionWords = 1024;   // 4 KB per warp: bitmap of 32,768 ranks
 constexpr uint32_t kDefaultStageSlots = 4;
 constexpr uint32_t kDefaultStageBytes = 1024;
 constexpr uint32_t kPlainRatio = 16;    // long/short above this -> search family (PLAIN)
@@ -154,208 +156,145 @@ __global__ void k_item_fill(const uint64_t *__restrict__ off, const uint64_t *__
     if (blockIdx.x == 0 && threadIdx.x == 0) acc[2] = base[n];
 }
 
-struct BlkCfg {
-    uint32_t E;           // in-edges per block item
-    uint32_t T;           // hash-table slots per block
-    uint32_t S;           // staging slots per warp
-    uint32_t slot_bytes;  // bytes per staging slot
-    uint32_t meta_off;    // byte offsets of the shared-memory regions
-    uint32_t tab_off;
-    uint32_t ring_off;
+struct WarpCfg {
+    uint32_t E;      // in-edges per item
+    uint32_t R;      // 32-bit words of the per-warp shared-memory region (bitmap or table)
+    uint32_t n;      // vertices of the counting form
 };
 
-constexpr uint32_t kBatch = 32;  // in-edges a warp takes from its block's item at a time
-
-// table size for a list of b elements: 4b slots rounded up to a power of two (load <= 1/4)
-// within [32, T]; b <= T/2 keeps the load at or below 1/2.
-__device__ __forceinline__ uint32_t table_lg(uint32_t b, uint32_t T) {
-    uint32_t lg = 5;
-    while ((1u << lg) < 4 * b && (1u << lg) < T) ++lg;
-    return lg;
+// Stream the suffix ranges of up to 32 in-edges (lane i holds edge i's [x, y)) in blocks of
+// 128 elements (4 coalesced 32-bit loads per lane), one block loaded ahead of the one being
+// tested. f(w) tests one element; it is called for valid elements only.
+template <class F>
+__device__ __forceinline__ unsigned long long stream_batch(const uint32_t *__restrict__ adj,
+                                                           uint32_t my_x, uint32_t my_y,
+                                                           uint32_t nb, int lane, F f) {
+    unsigned long long cnt = 0;
+    uint32_t e = 0;
+    uint32_t X = __shfl_sync(kFull, my_x, 0), Y = __shfl_sync(kFull, my_y, 0);
+    // skip to the first non-empty suffix
+    while (e < nb && X >= Y) {
+        ++e;
+        const uint32_t ee = e < nb ? e : 0u;
+        X = __shfl_sync(kFull, my_x, ee);
+        Y = __shfl_sync(kFull, my_y, ee);
+    }
+    if (e >= nb) return 0;
+    uint32_t c[4];
+    uint32_t cY = Y, cX = X;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        const uint32_t i = cX + lane + 32 * k;
+        c[k] = i < cY ? __ldg(adj + i) : kEmpty;
+    }
+    bool have = true;
+    while (have) {
+        // next block position
+        X += 128;
+        if (X >= Y) {
+            do {
+                ++e;
+                const uint32_t ee = e < nb ? e : 0u;
+                X = __shfl_sync(kFull, my_x, ee);
+                Y = __shfl_sync(kFull, my_y, ee);
+            } while (e < nb && X >= Y);
+        }
+        const bool more = e < nb;
+        uint32_t nx[4];
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            const uint32_t i = X + lane + 32 * k;
+            nx[k] = (more && i < Y) ? __ldg(adj + i) : kEmpty;
+        }
+#pragma unroll
+        for (int k = 0; k < 4; ++k)
+            if (c[k] != kEmpty) cnt += f(c[k]);
+#pragma unroll
+        for (int k = 0; k < 4; ++k) c[k] = nx[k];
+        have = more;
+    }
+    return cnt;
 }
 
 // acc[0] = total, acc[1] = item queue head, acc[2] = number of items
-__global__ void k_tc_block(const uint64_t *__restrict__ off, const uint32_t *__restrict__ adj,
-                           const uint64_t *__restrict__ in_off, const uint2 *__restrict__ in_rng,
-                           const uint64_t *__restrict__ items, unsigned long long *acc, BlkCfg p,
-                           uint32_t *status) {
-    extern __shared__ __align__(128) unsigned char smem[];
+__global__ void k_tc_warp(const uint64_t *__restrict__ off, const uint32_t *__restrict__ adj,
+                          const uint64_t *__restrict__ in_off, const uint2 *__restrict__ in_rng,
+                          const uint64_t *__restrict__ items, unsigned long long *acc,
+                          WarpCfg p) {
+    extern __shared__ __align__(16) uint32_t smem[];
     __shared__ unsigned long long red[32];
-    __shared__ uint32_t s_v, s_k0, s_next, s_stop;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    uint32_t *tab = reinterpret_cast<uint32_t *>(smem + p.tab_off);
-    uint64_t *bars = reinterpret_cast<uint64_t *>(smem) + (size_t)warp * p.S;
-    uint32_t *meta = reinterpret_cast<uint32_t *>(smem + p.meta_off) + (size_t)warp * p.S * 2;
-    unsigned char *ring = smem + p.ring_off + (size_t)warp * p.S * p.slot_bytes;
-    if ((uint32_t)lane < p.S) mbar_init(bars + lane, 1);
-    fence_mbar_init();
-    if (threadIdx.x == 0) s_stop = 0;
-    __syncthreads();
-    const uint32_t CH = p.slot_bytes / 4 - 4;  // list elements per staged chunk
+    uint32_t *reg = smem + (size_t)warp * p.R;
+    for (uint32_t q = lane; q < p.R; q += 32) reg[q] = 0u;  // the region is all-zero between items
+    __syncwarp();
+    const uint32_t RB = p.R * 32;  // bitmap capacity in bits
     const unsigned long long nitems = acc[2];
-    uint32_t phase = 0;                        // parity bit per staging slot
     unsigned long long cnt = 0;
-
     while (true) {
-        if (threadIdx.x == 0) {
-            const unsigned long long k = s_stop ? nitems : atomicAdd(&acc[1], 1ull);
-            if (k >= nitems) {
-                s_v = kEmpty;
-            } else {
-                const uint64_t it = items[k];
-                s_v = (uint32_t)(it >> 32);
-                s_k0 = (uint32_t)it;
-                s_next = (uint32_t)it;
-            }
-        }
-        __syncthreads();
-        const uint32_t v = s_v;
-        if (v == kEmpty) break;
+        unsigned long long k = 0;
+        if (lane == 0) k = atomicAdd(&acc[1], 1ull);
+        k = __shfl_sync(kFull, k, 0);
+        if (k >= nitems) break;
+        const uint64_t it = items[k];
+        const uint32_t v = (uint32_t)(it >> 32), k0 = (uint32_t)it;
         const uint64_t ov = off[v];
         const uint32_t b = (uint32_t)(off[v + 1] - ov);
         const uint64_t kin = in_off[v];
-        const uint32_t k1 = min(s_k0 + p.E, (uint32_t)(in_off[v + 1] - kin));
+        const uint32_t k1 = min(k0 + p.E, (uint32_t)(in_off[v + 1] - kin));
         const uint32_t *Nv = adj + ov;
-        const bool hashed = b <= p.T / 2;
-        uint32_t lg = 0, mask = 0;
-        if (hashed) {
-            lg = table_lg(b, p.T);
-            mask = (1u << lg) - 1;
-            uint4 *t4 = reinterpret_cast<uint4 *>(tab);
-            const uint4 e4 = make_uint4(kEmpty, kEmpty, kEmpty, kEmpty);
-            for (uint32_t q = threadIdx.x; q < (1u << lg) / 4; q += blockDim.x) t4[q] = e4;
-            __syncthreads();
-            for (uint32_t q = threadIdx.x; q < b; q += blockDim.x) {
+        const uint32_t window = p.n - 1 - v;  // every element of these lists lies in (v, n)
+        const int mode = (window <= RB) ? 0 : (2 * b <= p.R ? 1 : 2);  // bitmap / hash / merge
+        uint32_t lg = 0;
+        if (mode == 0) {
+            for (uint32_t q = lane; q < b; q += 32) {
+                const uint32_t o = __ldg(Nv + q) - v - 1;
+                atomicOr(&reg[o >> 5], 1u << (o & 31));
+            }
+        } else if (mode == 1) {
+            lg = 5;
+            while ((1u << lg) < 2 * b) ++lg;  // 2b <= R keeps (1 << lg) <= R for R a power of 2
+            for (uint32_t q = lane; q < (1u << lg); q += 32) reg[q] = kEmpty;
+            __syncwarp();
+            const uint32_t mask = (1u << lg) - 1;
+            for (uint32_t q = lane; q < b; q += 32) {
                 const uint32_t w = __ldg(Nv + q);
                 uint32_t sl = hash_slot(w, lg);
-                while (atomicCAS(&tab[sl], kEmpty, w) != kEmpty) sl = (sl + 1) & mask;
-            }
-            __syncthreads();
-        }
-
-        if (!hashed) {
-            // N+(v) too long for the table: tile merge of every suffix with N+(v)
-            while (true) {
-                uint32_t kb = 0;
-                if (lane == 0) kb = atomicAdd(&s_next, 1u);
-                kb = __shfl_sync(kFull, kb, 0);
-                if (kb >= k1) break;
-                const uint2 r = in_rng[kin + kb];
-                cnt += warp_merge_count(adj + r.x, r.y - r.x, Nv, b, lane);
-            }
-        } else {
-            // batches of in-edges: lane i holds the suffix range of edge kb + i; the next
-            // batch is taken and its ranges loaded while the current one is staged
-            auto take_batch = [&](uint32_t &kb, uint32_t &nb, uint2 &r) {
-                uint32_t x = 0;
-                if (lane == 0) x = atomicAdd(&s_next, kBatch);
-                kb = __shfl_sync(kFull, x, 0);
-                nb = kb < k1 ? min(kBatch, k1 - kb) : 0u;
-                r = ((uint32_t)lane < nb) ? __ldg(in_rng + kin + kb + lane) : make_uint2(0u, 0u);
-            };
-            uint32_t kb, nb, nkb, nnb;
-            uint2 my_r, nx_r;
-            take_batch(kb, nb, my_r);
-            take_batch(nkb, nnb, nx_r);
-            uint32_t e = 0;
-            uint32_t ex = __shfl_sync(kFull, my_r.x, 0), ey = __shfl_sync(kFull, my_r.y, 0);
-            bool done = nb == 0;
-            uint32_t inflight = 0, sw = 0, sr = 0;
-            bool failed = false;
-            while (true) {
-                while (inflight < p.S && !done) {
-                    uint32_t start = 0, len = 0;
-                    while (true) {
-                        if (e >= nb) {
-                            if (nnb == 0) {
-                                done = true;
-                                break;
-                            }
-                            kb = nkb;
-                            nb = nnb;
-                            my_r = nx_r;
-                            take_batch(nkb, nnb, nx_r);
-                            e = 0;
-                            ex = __shfl_sync(kFull, my_r.x, 0);
-                            ey = __shfl_sync(kFull, my_r.y, 0);
-                            continue;
-                        }
-                        if (ex < ey) {
-                            start = ex;
-                            len = min(CH, ey - ex);
-                            ex += len;
-                            break;
-                        }
-                        ++e;
-                        const uint32_t ee = e < nb ? e : 0u;
-                        ex = __shfl_sync(kFull, my_r.x, ee);
-                        ey = __shfl_sync(kFull, my_r.y, ee);
-                    }
-                    if (done) break;
-                    const uintptr_t ga = reinterpret_cast<uintptr_t>(adj + start);
-                    const uintptr_t gb = ga & ~(uintptr_t)15;
-                    const uint32_t head = (uint32_t)(ga - gb) >> 2;
-                    const uint32_t bytes = ((head + len) * 4u + 15u) & ~15u;
-                    if (lane == 0) {
-                        meta[2 * sw] = head;
-                        meta[2 * sw + 1] = len;
-                        mbar_arrive_expect_tx(bars + sw, bytes);
-                        bulk_copy_g2s(ring + (size_t)sw * p.slot_bytes,
-                                      reinterpret_cast<const void *>(gb), bytes, bars + sw);
-                    }
-                    sw = (sw + 1 == p.S) ? 0 : sw + 1;
-                    ++inflight;
-                }
-                if (inflight == 0) break;
-                __syncwarp();
-                if (!mbar_wait(bars + sr, (phase >> sr) & 1u)) {
-                    if (lane == 0) {
-                        atomicExch(status, kStatusTimeout);
-                        atomicExch(&s_stop, 1u);
-                    }
-                    for (uint32_t q = 1; q < inflight; ++q) {  // bounded drain of the others
-                        const uint32_t s2 = (sr + q) % p.S;
-                        mbar_wait(bars + s2, (phase >> s2) & 1u);
-                    }
-                    failed = true;
-                    break;
-                }
-                phase ^= 1u << sr;
-                const uint32_t head = meta[2 * sr], len = meta[2 * sr + 1];
-                const uint32_t *data =
-                    reinterpret_cast<const uint32_t *>(ring + (size_t)sr * p.slot_bytes) + head;
-                // every lane walks its own elements (t = lane, lane+32, ...) one probe step per
-                // round, so a long probe chain on one lane does not hold the others
-                uint32_t t = lane;
-                bool act = t < len;
-                uint32_t w = act ? data[t] : 0u;
-                uint32_t sl = act ? hash_slot(w, lg) : 0u;
-                while (__any_sync(kFull, act)) {
-                    if (act) {
-                        const uint32_t x = tab[sl];
-                        if (x == w || x == kEmpty) {
-                            cnt += (x == w);
-                            t += 32;
-                            act = t < len;
-                            if (act) {
-                                w = data[t];
-                                sl = hash_slot(w, lg);
-                            }
-                        } else {
-                            sl = (sl + 1) & mask;
-                        }
-                    }
-                }
-                __syncwarp();
-                fence_proxy_async_smem();
-                sr = (sr + 1 == p.S) ? 0 : sr + 1;
-                --inflight;
-            }
-            if (failed) {
-                // leave this item; s_stop ends the block after it
+                while (atomicCAS(&reg[sl], kEmpty, w) != kEmpty) sl = (sl + 1) & mask;
             }
         }
-        __syncthreads();  // the table is rebuilt for the next item
+        __syncwarp();
+        // batches of 32 in-edges; the ranges of the next batch are loaded one batch ahead
+        uint2 nxt = make_uint2(0u, 0u);
+        if (k0 + lane < k1) nxt = __ldg(in_rng + kin + k0 + lane);
+        for (uint32_t kb = k0; kb < k1; kb += 32) {
+            const uint2 my = nxt;
+            const uint32_t nb = min(32u, k1 - kb);
+            nxt = make_uint2(0u, 0u);
+            if (kb + 32 + lane < k1) nxt = __ldg(in_rng + kin + kb + 32 + lane);
+            if (mode == 0) {
+                const uint32_t base = v + 1;
+                cnt += stream_batch(adj, my.x, my.y, nb, lane, [&](uint32_t w) -> uint32_t {
+                    const uint32_t o = w - base;
+                    return (reg[o >> 5] >> (o & 31)) & 1u;
+                });
+            } else if (mode == 1) {
+                cnt += stream_batch(adj, my.x, my.y, nb, lane,
+                                    [&](uint32_t w) -> uint32_t { return hash_probe(reg, lg, w); });
+            } else {
+                for (uint32_t e = 0; e < nb; ++e) {
+                    const uint32_t x = __shfl_sync(kFull, my.x, e), y = __shfl_sync(kFull, my.y, e);
+                    cnt += warp_merge_count(adj + x, y - x, Nv, b, lane);
+                }
+            }
+        }
+        __syncwarp();
+        // return the region to all-zero
+        if (mode == 0) {
+            for (uint32_t q = lane; q < b; q += 32) reg[(__ldg(Nv + q) - v - 1) >> 5] = 0u;
+        } else if (mode == 1) {
+            for (uint32_t q = lane; q < (1u << lg); q += 32) reg[q] = 0u;
+        }
+        __syncwarp();
     }
     block_add_total(cnt, &acc[0], red);
 }
@@ -435,21 +374,11 @@ rtg_status batched_plan(rtg_ctx *ctx, rtg_graph *g, TcPlan **out) {
     if (!c.built)
         return bail(fail(ctx, RTG_ERR_STATE, "counting form of the CSR is missing"));
     const uint32_t E = cfg.tc_item_edges, W = cfg.tc_block_warps;
-    BlkCfg pc{};
+    WarpCfg pc{};
     pc.E = E;
-    // table: explicit size, else 4x the longest out-list (power of two) in [1024, 16384]
-    uint32_t T = cfg.tc_hash_slots;
-    if (!T) {
-        T = 1024;
-        while (T < 4ull * c.max_deg && T < 16384) T <<= 1;
-    }
-    pc.T = T;
-    pc.S = cfg.tc_stage_slots;
-    pc.slot_bytes = cfg.tc_stage_bytes;
-    pc.meta_off = W * pc.S * 8;
-    pc.tab_off = align128(pc.meta_off + W * pc.S * 8);
-    pc.ring_off = align128(pc.tab_off + pc.T * 4);
-    const size_t smem = (size_t)pc.ring_off + (size_t)W * pc.S * pc.slot_bytes;
+    pc.R = cfg.tc_hash_slots ? cfg.tc_hash_slots : kDefaultRegionWords;
+    pc.n = c.n;
+    const size_t smem = (size_t)W * pc.R * 4;
     if (smem + 256 > (size_t)ctx->smem_optin)
         return bail(fail(ctx, RTG_ERR_INVALID_ARG, "schedule needs %zu B of shared memory", smem));
 
@@ -468,11 +397,11 @@ rtg_status batched_plan(rtg_ctx *ctx, rtg_graph *g, TcPlan **out) {
     if ((e = cudaEventCreate(&p->k0)) != cudaSuccess ||
         (e = cudaEventCreate(&p->k1)) != cudaSuccess)
         return bail(cuda_fail(ctx, e, "event", __FILE__, __LINE__));
-    if ((e = cudaFuncSetAttribute(k_tc_block, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    if ((e = cudaFuncSetAttribute(k_tc_warp, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                   (int)smem)) != cudaSuccess)
         return bail(cuda_fail(ctx, e, "smem attribute", __FILE__, __LINE__));
     int per_sm = 0;
-    if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_tc_block, W * 32, smem)) !=
+    if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_tc_warp, W * 32, smem)) !=
         cudaSuccess)
         return bail(cuda_fail(ctx, e, "occupancy", __FILE__, __LINE__));
     if (cfg.tc_blocks_per_sm) per_sm = std::min<int>(per_sm, (int)cfg.tc_blocks_per_sm);
@@ -491,8 +420,8 @@ rtg_status batched_plan(rtg_ctx *ctx, rtg_graph *g, TcPlan **out) {
                                   ctx->stream);
     k_item_fill<<<g1, 256, 0, ctx->stream>>>(c.off, c.in_off, c.n, E, vbase, p->items, p->acc);
     cudaEventRecordWithFlags(p->k0, ctx->stream, cudaEventRecordExternal);
-    k_tc_block<<<grid, W * 32, smem, ctx->stream>>>(c.off, c.adj, c.in_off, c.in_rng, p->items,
-                                                    p->acc, pc, ctx->d_status);
+    k_tc_warp<<<grid, W * 32, smem, ctx->stream>>>(c.off, c.adj, c.in_off, c.in_rng, p->items,
+                                                   p->acc, pc);
     cudaEventRecordWithFlags(p->k1, ctx->stream, cudaEventRecordExternal);
     e = cudaStreamEndCapture(ctx->stream, &p->graph);
     if (e != cudaSuccess) return bail(cuda_fail(ctx, e, "end capture", __FILE__, __LINE__));
