@@ -211,6 +211,32 @@ rtg_status rtg_tc_count_host_edges(rtg_ctx *ctx, const uint32_t *src, const uint
 rtg_status rtg_tc_count_host_csr(rtg_ctx *ctx, const int32_t *offsets, const int32_t *adjs,
                                  int32_t nodes, int64_t edges, rtg_tc_mode mode,
                                  uint64_t *out_total, rtg_timing *timing);
+/* Allocation-free triangle count. No counterpart in the reference: it exists for callers
+ * that cannot let a library call cudaMalloc, for example code running inside an
+ * application whose memory pool or framework allocator owns the device heap, or code on a
+ * latency-critical path where the implicit device synchronisation of an allocation is not
+ * allowed. It needs no rtg_ctx.
+ *
+ * Input: an oriented CSR already on the current device (d_offsets: n+1 entries, d_adj: m
+ * entries, rows sorted ascending, every edge stored once). Output: the exact uint64
+ * triangle count written to the host word *out_total. Work is ordered on `stream`
+ * (a cudaStream_t; NULL for the default stream) and the call returns when the count is
+ * on the host. It uses the PLAIN kernels; their scratch lives in one fixed device array
+ * inside the library (about 9 bytes per edge for RTG_NOALLOC_MAX_EDGES edges, reserved on
+ * every GPU that loads the library until the process exits), so:
+ *   - graphs with more than RTG_NOALLOC_MAX_EDGES edges are rejected with
+ *     RTG_ERR_INVALID_ARG before any GPU work, as are offsets that do not describe a CSR of
+ *     m edges with ids below n;
+ *   - the first call on a device looks up the array's device address (once per device, with
+ *     that device current); make that first call before any stream capture;
+ *   - every call on a device shares the one array, so calls that overlap on the GPU (other
+ *     host threads, other streams) race and must be serialised by the caller.
+ * Returns RTG_ERR_DEVICE on a CUDA error. It calls no cudaMalloc, cudaFree or other
+ * allocating routine. */
+#define RTG_NOALLOC_MAX_EDGES (1u << 19)
+rtg_status rtg_tc_count_device_csr_noalloc(const uint64_t *d_offsets, const uint32_t *d_adj,
+                                           uint32_t n, uint64_t m, uint64_t *out_total,
+                                           void *stream);
 /* |N(u) ∩ N(v)| on the symmetric CSR for each query pair (u[i], v[i]). */
 rtg_status rtg_graph_pair_count(rtg_ctx *ctx, rtg_graph *g, const uint32_t *u,
                                 const uint32_t *v, uint64_t npairs, uint32_t *out,

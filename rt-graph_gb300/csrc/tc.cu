@@ -26,6 +26,7 @@
 #include <cub/cub.cuh>
 
 #include <algorithm>
+#include <mutex>
 
 #include "internal.h"
 #include "intersect.cuh"
@@ -565,4 +566,140 @@ rtg_status tc_count(rtg_ctx *ctx, rtg_graph *g, rtg_tc_mode mode, uint64_t *tota
     return count_batched(ctx, g, total, t);
 }
 
+// ------------------------------------------------------ allocation-free entry point
+//
+// For callers that must not allocate device memory: code running while another component
+// owns the device heap (a framework's caching allocator, a memory pool handed out by the
+// host application), code on a path where an allocation's implicit device synchronisation
+// is not allowed, or code that may not grow the process's GPU footprint after start-up.
+// The PLAIN count runs with its per-edge scratch (edge sources, bucket ids, bucket lists)
+// and its counters placed in one file-scope device array instead of cudaMalloc'd buffers.
+
+namespace {
+
+constexpr uint64_t kNoAllocMaxEdges = RTG_NOALLOC_MAX_EDGES;
+constexpr size_t kNoAllocCounterBytes = 256;  // total, status, bucket counts/bases/cursors
+constexpr size_t kNoAllocScratchBytes =
+    kNoAllocCounterBytes + kNoAllocMaxEdges * (4 /*src*/ + 4 /*lists*/ + 1 /*bucket*/);
+
+// Shared by every call on a device and kept between calls; held by every GPU that loads
+// the library until the process exits.
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
+
+std::mutex g_noalloc_mu;
+void *g_noalloc_addr[256] = {};
+
+__global__ void k_noalloc_check(const uint64_t *__restrict__ off, const uint32_t *__restrict__ adj,
+                                uint32_t n, uint64_t m, uint32_t *status) {
+    for (uint64_t v = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; v <= n;
+         v += (uint64_t)gridDim.x * blockDim.x) {
+        const uint64_t o = off[v];
+        if (o > m || (v == 0 && o != 0) || (v == n && o != m) || (v < n && off[v + 1] < o))
+            atomicExch(status, 1u);
+    }
+    for (uint64_t e = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; e < m;
+         e += (uint64_t)gridDim.x * blockDim.x)
+        if (adj[e] >= n) atomicExch(status, 1u);
+}
+
+__global__ void k_noalloc_src(const uint64_t *__restrict__ off, uint32_t n, uint32_t *src) {
+    for (uint64_t v = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; v < n;
+         v += (uint64_t)gridDim.x * blockDim.x)
+        for (uint64_t e = off[v]; e < off[v + 1]; ++e) src[e] = (uint32_t)v;
+}
+
+}  // namespace
+
 }  // namespace rtg
+
+using namespace rtg;
+
+extern "C" rtg_status rtg_tc_count_device_csr_noalloc(const uint64_t *d_offsets,
+                                                       const uint32_t *d_adj, uint32_t n,
+                                                       uint64_t m, uint64_t *out_total,
+                                                       void *stream) {
+    if (!out_total || (n && !d_offsets) || (m && !d_adj)) return RTG_ERR_INVALID_ARG;
+    if (m > kNoAllocMaxEdges || n > 0x7FFFFFFEu) return RTG_ERR_INVALID_ARG;
+    *out_total = 0;
+    if (m == 0 || n == 0) return RTG_OK;
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 256) {
+        cudaGetLastError();
+        return RTG_ERR_DEVICE;
+    }
+    void *base = nullptr;
+    {
+        // set-up, once per device, with that device current: the array's device address
+        std::lock_guard<std::mutex> lk(g_noalloc_mu);
+        if (!g_noalloc_addr[dev]) {
+            void *p = nullptr;
+            if (cudaGetSymbolAddress(&p, g_noalloc_scratch) != cudaSuccess || !p) {
+                cudaGetLastError();
+                return RTG_ERR_DEVICE;
+            }
+            g_noalloc_addr[dev] = p;
+        }
+        base = g_noalloc_addr[dev];
+    }
+    cudaStream_t st = (cudaStream_t)stream;
+    unsigned char *b = (unsigned char *)base;
+    unsigned long long *d_total = (unsigned long long *)b;
+    uint32_t *d_status = (uint32_t *)(b + 8);
+    unsigned long long *d_counts = (unsigned long long *)(b + 16);
+    unsigned long long *d_base = d_counts + kPlainBuckets;
+    unsigned long long *d_cursor = d_base + kPlainBuckets;
+    uint32_t *d_src = (uint32_t *)(b + kNoAllocCounterBytes);
+    uint32_t *d_lists = d_src + kNoAllocMaxEdges;
+    uint8_t *d_bucket = (uint8_t *)(d_lists + kNoAllocMaxEdges);
+    auto cuda_ok = [](cudaError_t e) {
+        if (e == cudaSuccess) return true;
+        cudaGetLastError();
+        return false;
+    };
+    int sms = 0;
+    if (!cuda_ok(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev))) return RTG_ERR_DEVICE;
+    const int grid = (int)std::max<uint64_t>(1, std::min<uint64_t>((m + n + 255) / 256, sms * 16ull));
+    // counters start at zero on every call (the array keeps the previous call's contents)
+    if (!cuda_ok(cudaMemsetAsync(b, 0, kNoAllocCounterBytes, st))) return RTG_ERR_DEVICE;
+    k_noalloc_check<<<grid, 256, 0, st>>>(d_offsets, d_adj, n, m, d_status);
+    uint32_t bad = 0;
+    if (!cuda_ok(cudaGetLastError()) ||
+        !cuda_ok(cudaMemcpyAsync(&bad, d_status, 4, cudaMemcpyDeviceToHost, st)) ||
+        !cuda_ok(cudaStreamSynchronize(st)))
+        return RTG_ERR_DEVICE;
+    if (bad) return RTG_ERR_INVALID_ARG;  // offsets not a CSR of m edges, or ids >= n
+    k_noalloc_src<<<grid, 256, 0, st>>>(d_offsets, n, d_src);
+    k_plain_classify<<<grid, 256, 0, st>>>(d_offsets, d_adj, d_src, m, d_bucket, d_counts);
+    unsigned long long hc[kPlainBuckets] = {0};
+    if (!cuda_ok(cudaGetLastError()) ||
+        !cuda_ok(cudaMemcpyAsync(hc, d_counts, sizeof hc, cudaMemcpyDeviceToHost, st)) ||
+        !cuda_ok(cudaStreamSynchronize(st)))
+        return RTG_ERR_DEVICE;
+    unsigned long long hb[kPlainBuckets], run = 0;
+    for (int i = 0; i < kPlainBuckets; ++i) {
+        hb[i] = run;
+        run += hc[i];
+    }
+    if (run) {
+        if (!cuda_ok(cudaMemcpyAsync(d_base, hb, sizeof hb, cudaMemcpyHostToDevice, st)))
+            return RTG_ERR_DEVICE;
+        k_plain_scatter<<<grid, 256, 0, st>>>(d_bucket, m, d_base, d_cursor, d_lists);
+        for (int i = 0; i < kPlainBuckets; ++i) {
+            if (!hc[i]) continue;
+            const int gb = (int)std::min<uint64_t>((hc[i] + 7) / 8, 65535);
+            if (i < 3)
+                k_plain_edges<false><<<gb, 256, 0, st>>>(d_offsets, d_adj, d_src, d_lists + hb[i],
+                                                         hc[i], d_total);
+            else
+                k_plain_edges<true><<<gb, 256, 0, st>>>(d_offsets, d_adj, d_src, d_lists + hb[i],
+                                                        hc[i], d_total);
+        }
+    }
+    unsigned long long h = 0;
+    if (!cuda_ok(cudaGetLastError()) ||
+        !cuda_ok(cudaMemcpyAsync(&h, d_total, 8, cudaMemcpyDeviceToHost, st)) ||
+        !cuda_ok(cudaStreamSynchronize(st)))
+        return RTG_ERR_DEVICE;
+    *out_total = h;
+    return RTG_OK;
+}
