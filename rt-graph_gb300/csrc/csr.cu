@@ -91,19 +91,28 @@ __global__ void k_sym_keys(const uint64_t *ukeys, uint64_t m, int B, uint64_t *o
     }
 }
 
-// adj/src from sorted keys, offsets from the row boundaries
-__global__ void k_csr_fill(const uint64_t *keys, uint64_t m, int B, uint32_t n, uint32_t *adj,
-                           uint32_t *src, uint64_t *off) {
+// row offsets of keys sorted by (key >> shift): off[x] = first i with (keys[i] >> shift) >= x
+__global__ void k_row_offsets(const uint64_t *keys, uint64_t m, int shift, uint32_t n,
+                              uint64_t *off) {
+    GRID_STRIDE(x, (uint64_t)n + 1) {
+        uint64_t lo = 0, hi = m;
+        while (lo < hi) {
+            const uint64_t mid = (lo + hi) >> 1;
+            if ((keys[mid] >> shift) < x) lo = mid + 1;
+            else hi = mid;
+        }
+        off[x] = lo;
+    }
+}
+
+// adj/src from sorted keys
+__global__ void k_csr_fill(const uint64_t *keys, uint64_t m, int B, uint32_t *adj,
+                           uint32_t *src) {
     const uint64_t lo_mask = (1ull << B) - 1;
     GRID_STRIDE(i, m) {
-        uint64_t k = keys[i];
-        uint32_t s = (uint32_t)(k >> B);
+        const uint64_t k = keys[i];
         adj[i] = (uint32_t)(k & lo_mask);
-        if (src) src[i] = s;
-        int64_t prev = (i == 0) ? -1 : (int64_t)(keys[i - 1] >> B);
-        for (int64_t v = prev + 1; v <= (int64_t)s; ++v) off[v] = i;
-        if (i == m - 1)
-            for (uint64_t v = (uint64_t)s + 1; v <= n; ++v) off[v] = m;
+        if (src) src[i] = (uint32_t)(k >> B);
     }
 }
 
@@ -241,9 +250,9 @@ rtg_status fill_csr(rtg_ctx *ctx, const uint64_t *keys, uint64_t m, int B, uint3
     if (m == 0) {
         RTG_CUDA(ctx, cudaMemsetAsync(c.off, 0, (n + 1ull) * 8, ctx->stream));
     } else {
-        k_csr_fill<<<grid_for(ctx, m), kThreads, 0, ctx->stream>>>(keys, m, B, n, c.adj, c.src,
-                                                                    c.off);
-        ctx->launches++;
+        k_csr_fill<<<grid_for(ctx, m), kThreads, 0, ctx->stream>>>(keys, m, B, c.adj, c.src);
+        k_row_offsets<<<grid_for(ctx, n + 1ull), kThreads, 0, ctx->stream>>>(keys, m, B, n, c.off);
+        ctx->launches += 2;
         RTG_CUDA(ctx, cudaGetLastError());
     }
     unsigned long long *w = ctx->d_scalars;
@@ -329,16 +338,11 @@ __global__ void k_in_keys(const uint32_t *adj_r, uint64_t m, uint64_t *keys) {
     GRID_STRIDE(e, m) { keys[e] = ((uint64_t)adj_r[e] << 32) | (uint32_t)e; }
 }
 
-__global__ void k_in_fill(const uint64_t *keys, uint64_t m, uint32_t n, const uint64_t *off_r,
-                          const uint32_t *src_r, uint2 *rng, uint64_t *in_off) {
+__global__ void k_in_fill(const uint64_t *keys, uint64_t m, const uint64_t *off_r,
+                          const uint32_t *src_r, uint2 *rng) {
     GRID_STRIDE(i, m) {
-        const uint64_t k = keys[i];
-        const uint32_t v = (uint32_t)(k >> 32), e = (uint32_t)k;
+        const uint32_t e = (uint32_t)keys[i];
         rng[i] = make_uint2(e + 1, (uint32_t)off_r[src_r[e] + 1]);
-        const int64_t prev = (i == 0) ? -1 : (int64_t)(keys[i - 1] >> 32);
-        for (int64_t x = prev + 1; x <= (int64_t)v; ++x) in_off[x] = i;
-        if (i == m - 1)
-            for (uint64_t x = (uint64_t)v + 1; x <= n; ++x) in_off[x] = m;
     }
 }
 
@@ -413,15 +417,18 @@ rtg_status csr_build_count(rtg_ctx *ctx, const Csr &c, CountCsr &cc) {
         cc.built = true;
         return RTG_OK;
     }
-    k_csr_fill<<<grid_for(ctx, mr), kThreads, 0, ctx->stream>>>(ek, mr, B, n, cc.adj, src_r, cc.off);
+    k_csr_fill<<<grid_for(ctx, mr), kThreads, 0, ctx->stream>>>(ek, mr, B, cc.adj, src_r);
+    k_row_offsets<<<grid_for(ctx, n + 1ull), kThreads, 0, ctx->stream>>>(ek, mr, B, n, cc.off);
     k_in_keys<<<grid_for(ctx, mr), kThreads, 0, ctx->stream>>>(cc.adj, mr, other);
-    ctx->launches += 2;
+    ctx->launches += 3;
     RTG_CUDA(ctx, cudaGetLastError());
     cub::DoubleBuffer<uint64_t> di(other, ek);
     RTG_TRY(radix_sort(ctx, di, mr, std::min(64, 32 + B)));
-    k_in_fill<<<grid_for(ctx, mr), kThreads, 0, ctx->stream>>>(di.Current(), mr, n, cc.off, src_r,
-                                                                cc.in_rng, cc.in_off);
-    ctx->launches++;
+    k_in_fill<<<grid_for(ctx, mr), kThreads, 0, ctx->stream>>>(di.Current(), mr, cc.off, src_r,
+                                                                cc.in_rng);
+    k_row_offsets<<<grid_for(ctx, n + 1ull), kThreads, 0, ctx->stream>>>(di.Current(), mr, 32, n,
+                                                                          cc.in_off);
+    ctx->launches += 2;
     RTG_CUDA(ctx, cudaGetLastError());
     unsigned long long *w = ctx->d_scalars;
     RTG_CUDA(ctx, cudaMemsetAsync(w, 0, 16, ctx->stream));

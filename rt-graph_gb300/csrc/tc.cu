@@ -36,7 +36,7 @@ namespace rtg {
 
 namespace {
 
-constexpr uint32_t kDefaultItemEdges = 64;
+constexpr uint32_t kDefaultItemEdges = 256;
 constexpr uint32_t kDefaultBlockWarps = 8;
 constexpr uint32_t kDefaultRegionWords = 1024;   // 4 KB per warp: bitmap of 32,768 ranks
 constexpr uint32_t kDefaultStageSlots = 4;
@@ -85,15 +85,39 @@ __global__ void k_plain_classify(const uint64_t *__restrict__ off, const uint32_
         atomicAdd(&counts[threadIdx.x], (unsigned long long)local[threadIdx.x]);
 }
 
+// Scatter edge ids into their bucket lists. Positions are reserved per tile of
+// blockDim * kScatterPerThread edges: shared-memory counters rank the tile's edges within
+// each bucket, then one global atomicAdd per (tile, bucket) reserves their range.
+constexpr int kScatterPerThread = 16;
+
 __global__ void k_plain_scatter(const uint8_t *__restrict__ bucket, uint64_t m,
                                 const unsigned long long *__restrict__ base,
                                 unsigned long long *cursor, uint32_t *lists) {
-    for (uint64_t e = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; e < m;
-         e += (uint64_t)gridDim.x * blockDim.x) {
-        uint8_t id = bucket[e];
-        if (id == 0xFF) continue;
-        unsigned long long p = atomicAdd(&cursor[id], 1ull);
-        lists[base[id] + p] = (uint32_t)e;
+    __shared__ unsigned int cnt[kPlainBuckets];
+    __shared__ unsigned long long pos[kPlainBuckets];
+    const uint64_t tile = (uint64_t)blockDim.x * kScatterPerThread;
+    for (uint64_t t0 = blockIdx.x * tile; t0 < m; t0 += (uint64_t)gridDim.x * tile) {
+        if (threadIdx.x < kPlainBuckets) cnt[threadIdx.x] = 0;
+        __syncthreads();
+        uint8_t id[kScatterPerThread];
+        unsigned int rank[kScatterPerThread];
+#pragma unroll
+        for (int k = 0; k < kScatterPerThread; ++k) {
+            const uint64_t e = t0 + (uint64_t)k * blockDim.x + threadIdx.x;
+            id[k] = e < m ? bucket[e] : (uint8_t)0xFF;
+            rank[k] = id[k] != 0xFF ? atomicAdd(&cnt[id[k]], 1u) : 0u;
+        }
+        __syncthreads();
+        if (threadIdx.x < kPlainBuckets && cnt[threadIdx.x])
+            pos[threadIdx.x] = base[threadIdx.x] +
+                               atomicAdd(&cursor[threadIdx.x], (unsigned long long)cnt[threadIdx.x]);
+        __syncthreads();
+#pragma unroll
+        for (int k = 0; k < kScatterPerThread; ++k) {
+            const uint64_t e = t0 + (uint64_t)k * blockDim.x + threadIdx.x;
+            if (id[k] != 0xFF) lists[pos[id[k]] + rank[k]] = (uint32_t)e;
+        }
+        __syncthreads();
     }
 }
 
@@ -163,57 +187,67 @@ struct WarpCfg {
     uint32_t n;      // vertices of the counting form
 };
 
-// Stream the suffix ranges of up to 32 in-edges (lane i holds edge i's [x, y)) in blocks of
-// 128 elements (4 coalesced 32-bit loads per lane), one block loaded ahead of the one being
-// tested. f(w) tests one element; it is called for valid elements only.
+// Stream the suffix ranges of the item's in-edges [k0, k1) (edge k's range is in_rng[kin+k])
+// as a sequence of 32-element blocks, one coalesced 32-bit load per lane per block; a block
+// never spans two suffixes. kDepth blocks are in flight ahead of the block being tested, and
+// the pipeline runs across edge and batch boundaries; the ranges of the next 32 in-edges
+// are loaded one batch ahead. f(w) tests one element (valid elements only).
+constexpr int kDepth = 8;
+
 template <class F>
-__device__ __forceinline__ unsigned long long stream_batch(const uint32_t *__restrict__ adj,
-                                                           uint32_t my_x, uint32_t my_y,
-                                                           uint32_t nb, int lane, F f) {
+__device__ __forceinline__ unsigned long long stream_item(const uint32_t *__restrict__ adj,
+                                                          const uint2 *__restrict__ rng,
+                                                          uint32_t k0, uint32_t k1, int lane,
+                                                          F f) {
     unsigned long long cnt = 0;
+    uint32_t kb = k0;
+    uint32_t nb = min(32u, k1 - kb);
+    uint2 my = (kb + lane < k1) ? __ldg(rng + kb + lane) : make_uint2(0u, 0u);
+    uint2 nx = (kb + 32 + lane < k1) ? __ldg(rng + kb + 32 + lane) : make_uint2(0u, 0u);
     uint32_t e = 0;
-    uint32_t X = __shfl_sync(kFull, my_x, 0), Y = __shfl_sync(kFull, my_y, 0);
-    // skip to the first non-empty suffix
-    while (e < nb && X >= Y) {
-        ++e;
-        const uint32_t ee = e < nb ? e : 0u;
-        X = __shfl_sync(kFull, my_x, ee);
-        Y = __shfl_sync(kFull, my_y, ee);
-    }
-    if (e >= nb) return 0;
-    uint32_t c[4];
-    uint32_t cY = Y, cX = X;
-#pragma unroll
-    for (int k = 0; k < 4; ++k) {
-        const uint32_t i = cX + lane + 32 * k;
-        c[k] = i < cY ? __ldg(adj + i) : kEmpty;
-    }
-    bool have = true;
-    while (have) {
-        // next block position
-        X += 128;
-        if (X >= Y) {
-            do {
-                ++e;
-                const uint32_t ee = e < nb ? e : 0u;
-                X = __shfl_sync(kFull, my_x, ee);
-                Y = __shfl_sync(kFull, my_y, ee);
-            } while (e < nb && X >= Y);
+    uint32_t X = __shfl_sync(kFull, my.x, 0), Y = __shfl_sync(kFull, my.y, 0);
+    bool live = true;
+    // move (e, X, Y) to the next edge with elements left; warp-uniform
+    auto settle = [&]() {
+        while (live && X >= Y) {
+            if (++e >= nb) {
+                kb += 32;
+                if (kb >= k1) {
+                    live = false;
+                    break;
+                }
+                nb = min(32u, k1 - kb);
+                my = nx;
+                nx = (kb + 32 + lane < k1) ? __ldg(rng + kb + 32 + lane) : make_uint2(0u, 0u);
+                e = 0;
+            }
+            X = __shfl_sync(kFull, my.x, e);
+            Y = __shfl_sync(kFull, my.y, e);
         }
-        const bool more = e < nb;
-        uint32_t nx[4];
+    };
+    auto next_block = [&]() -> uint32_t {
+        if (!live) return kEmpty;
+        const uint32_t i = X + lane;
+        const uint32_t w = i < Y ? __ldg(adj + i) : kEmpty;
+        X += 32;
+        settle();
+        return w;
+    };
+    settle();
+    uint32_t buf[kDepth];
 #pragma unroll
-        for (int k = 0; k < 4; ++k) {
-            const uint32_t i = X + lane + 32 * k;
-            nx[k] = (more && i < Y) ? __ldg(adj + i) : kEmpty;
+    for (int d = 0; d < kDepth; ++d) buf[d] = next_block();
+    while (live) {
+#pragma unroll
+        for (int d = 0; d < kDepth; ++d) {
+            const uint32_t w = buf[d];
+            if (w != kEmpty) cnt += f(w);
+            buf[d] = next_block();
         }
-#pragma unroll
-        for (int k = 0; k < 4; ++k)
-            if (c[k] != kEmpty) cnt += f(c[k]);
-#pragma unroll
-        for (int k = 0; k < 4; ++k) c[k] = nx[k];
-        have = more;
     }
+#pragma unroll
+    for (int d = 0; d < kDepth; ++d)
+        if (buf[d] != kEmpty) cnt += f(buf[d]);
     return cnt;
 }
 
@@ -264,28 +298,19 @@ __global__ void k_tc_warp(const uint64_t *__restrict__ off, const uint32_t *__re
             }
         }
         __syncwarp();
-        // batches of 32 in-edges; the ranges of the next batch are loaded one batch ahead
-        uint2 nxt = make_uint2(0u, 0u);
-        if (k0 + lane < k1) nxt = __ldg(in_rng + kin + k0 + lane);
-        for (uint32_t kb = k0; kb < k1; kb += 32) {
-            const uint2 my = nxt;
-            const uint32_t nb = min(32u, k1 - kb);
-            nxt = make_uint2(0u, 0u);
-            if (kb + 32 + lane < k1) nxt = __ldg(in_rng + kin + kb + 32 + lane);
-            if (mode == 0) {
-                const uint32_t base = v + 1;
-                cnt += stream_batch(adj, my.x, my.y, nb, lane, [&](uint32_t w) -> uint32_t {
-                    const uint32_t o = w - base;
-                    return (reg[o >> 5] >> (o & 31)) & 1u;
-                });
-            } else if (mode == 1) {
-                cnt += stream_batch(adj, my.x, my.y, nb, lane,
-                                    [&](uint32_t w) -> uint32_t { return hash_probe(reg, lg, w); });
-            } else {
-                for (uint32_t e = 0; e < nb; ++e) {
-                    const uint32_t x = __shfl_sync(kFull, my.x, e), y = __shfl_sync(kFull, my.y, e);
-                    cnt += warp_merge_count(adj + x, y - x, Nv, b, lane);
-                }
+        if (mode == 0) {
+            const uint32_t base = v + 1;
+            cnt += stream_item(adj, in_rng + kin, k0, k1, lane, [&](uint32_t w) -> uint32_t {
+                const uint32_t o = w - base;
+                return (reg[o >> 5] >> (o & 31)) & 1u;
+            });
+        } else if (mode == 1) {
+            cnt += stream_item(adj, in_rng + kin, k0, k1, lane,
+                               [&](uint32_t w) -> uint32_t { return hash_probe(reg, lg, w); });
+        } else {
+            for (uint32_t kk = k0; kk < k1; ++kk) {
+                const uint2 r = __ldg(in_rng + kin + kk);
+                cnt += warp_merge_count(adj + r.x, r.y - r.x, Nv, b, lane);
             }
         }
         __syncwarp();
