@@ -90,12 +90,18 @@ typedef enum rtg_orient {
  *            CUDA graph, schedule from the context configuration (autotuned). */
 typedef enum rtg_tc_mode { RTG_TC_PLAIN = 0, RTG_TC_BATCHED = 1 } rtg_tc_mode;
 
-/* Set-intersection kernel families (flags of rtg_si_count*). AUTO picks per pair by
- * the length ratio. The forced families back the reference's per-baseline CLIs. */
+/* Set-intersection execution forms (flags of rtg_si_count*).
+ *  AUTO   : BATCHED form — one persistent launch; both lists of every pair (or of every
+ *           chunk pair of a long pair) are staged into shared memory by bulk copies and
+ *           merged there, several pairs in flight per warp.
+ *  PLAIN  : per-pair family from global memory: SEARCH when |long| > si_search_ratio *
+ *           |short|, MERGE otherwise.
+ *  FORCE_*: one family for every pair; these back the reference's per-baseline CLIs. */
 #define RTG_SI_AUTO 0u
 #define RTG_SI_FORCE_MERGE 1u   /* warp merge path (ip.cu)                        */
 #define RTG_SI_FORCE_SEARCH 2u  /* short list searched in the long list (bs.cu)   */
 #define RTG_SI_FORCE_BITMAP 3u  /* block bitmap / hash probe (bi_dynamic.cu, hi.cu) */
+#define RTG_SI_PLAIN 4u
 #define RTG_SI_FAMILY_MASK 0xFu
 #define RTG_PAIRS_DEVICE 0x100u /* pair arrays are device pointers                 */
 #define RTG_OUT_DEVICE 0x200u   /* output array is a device pointer                */
@@ -133,16 +139,16 @@ typedef struct rtg_graph_info {
 typedef struct rtg_config {
     uint32_t tc_block_warps;    /* warps per block of the persistent TC kernel        */
     uint32_t tc_item_edges;     /* in-edges of one vertex per work item               */
-    uint32_t tc_hash_slots;     /* shared-memory hash slots per block (power of two;
-                                   0 = 4x the longest out-list, within [1024, 16384]) */
+    uint32_t tc_region_words;   /* 32-bit words of shared memory per warp for the
+                                   out-list of the item's vertex: a bitmap of 32x that
+                                   many ranks, or a hash table (power of two, 64..16384) */
     uint32_t tc_blocks_per_sm;  /* resident blocks per SM of the persistent kernel    */
-    uint32_t tc_stage_slots;    /* bulk-copy staging slots per warp (2..16)           */
-    uint32_t tc_stage_bytes;    /* bytes per staging slot (multiple of 128, >= 256)   */
     uint32_t si_block_warps;    /* warps per block of the SI kernels                  */
-    uint32_t si_search_ratio;   /* long/short length ratio above which SEARCH is used */
-    uint32_t si_split_len;      /* pairs with |A|+|B| above this are split by merge
-                                   path across warps                                  */
-    uint32_t si_pairs_per_grab; /* pairs a warp takes from the queue per fetch        */
+    uint32_t si_search_ratio;   /* long/short length ratio above which the forced-
+                                   family-free PLAIN form uses SEARCH                 */
+    uint32_t si_stage_slots;    /* bulk-copy staging slots per warp (2..16)           */
+    uint32_t si_stage_bytes;    /* bytes per staging slot (multiple of 128, 512..32768) */
+    uint32_t si_blocks_per_sm;  /* resident blocks per SM of the batched SI kernel    */
 } rtg_config;
 
 /* ---------------------------------------------------------------- context */

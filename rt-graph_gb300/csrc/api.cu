@@ -176,18 +176,18 @@ void rtg_destroy(rtg_ctx *ctx) {
 
 rtg_status rtg_set_config(rtg_ctx *ctx, const rtg_config *cfg) {
     if (!ctx || !cfg) return RTG_ERR_INVALID_ARG;
-    if (cfg->tc_hash_slots && (cfg->tc_hash_slots & (cfg->tc_hash_slots - 1)))
-        return fail(ctx, RTG_ERR_INVALID_ARG, "tc_hash_slots must be a power of two");
-    if (cfg->tc_hash_slots && (cfg->tc_hash_slots < 64 || cfg->tc_hash_slots > 16384))
-        return fail(ctx, RTG_ERR_INVALID_ARG, "tc_hash_slots must be in [64, 16384]");
+    if (cfg->tc_region_words && (cfg->tc_region_words & (cfg->tc_region_words - 1)))
+        return fail(ctx, RTG_ERR_INVALID_ARG, "tc_region_words must be a power of two");
+    if (cfg->tc_region_words && (cfg->tc_region_words < 64 || cfg->tc_region_words > 16384))
+        return fail(ctx, RTG_ERR_INVALID_ARG, "tc_region_words must be in [64, 16384]");
     if (cfg->tc_block_warps > 32 || cfg->si_block_warps > 32)
         return fail(ctx, RTG_ERR_INVALID_ARG, "at most 32 warps per block");
-    if (cfg->tc_stage_slots && (cfg->tc_stage_slots < 2 || cfg->tc_stage_slots > 16))
-        return fail(ctx, RTG_ERR_INVALID_ARG, "tc_stage_slots must be in [2, 16]");
-    if (cfg->tc_stage_bytes && (cfg->tc_stage_bytes < 256 || cfg->tc_stage_bytes % 128 ||
-                                cfg->tc_stage_bytes > 65536))
+    if (cfg->si_stage_slots && (cfg->si_stage_slots < 2 || cfg->si_stage_slots > 16))
+        return fail(ctx, RTG_ERR_INVALID_ARG, "si_stage_slots must be in [2, 16]");
+    if (cfg->si_stage_bytes && (cfg->si_stage_bytes < 512 || cfg->si_stage_bytes % 128 ||
+                                cfg->si_stage_bytes > 32768))
         return fail(ctx, RTG_ERR_INVALID_ARG,
-                    "tc_stage_bytes must be a multiple of 128 in [256, 65536]");
+                    "si_stage_bytes must be a multiple of 128 in [512, 32768]");
     ctx->cfg = *cfg;
     return RTG_OK;
 }
@@ -656,7 +656,12 @@ rtg_status rtg_sets_from_host(rtg_ctx *ctx, const uint64_t *offsets, uint64_t ns
     s->nsets = nsets;
     s->nelems = ne;
     rtg_status st = dev_alloc(ctx, (void **)&s->off, (nsets + 1) * 8);
-    if (st == RTG_OK) st = dev_alloc(ctx, (void **)&s->elems, ne * 4);
+    // tail padding: staged copies widen a list's byte range to 16-byte boundaries
+    if (st == RTG_OK) st = dev_alloc(ctx, (void **)&s->elems, ne * 4 + kAdjPadBytes);
+    if (st == RTG_OK) {
+        cudaError_t pe = cudaMemsetAsync((char *)s->elems + ne * 4, 0, kAdjPadBytes, ctx->stream);
+        if (pe != cudaSuccess) st = cuda_fail(ctx, pe, "pad", __FILE__, __LINE__);
+    }
     cudaError_t e = cudaSuccess;
     if (st == RTG_OK) {
         e = cudaMemcpyAsync(s->off, offsets, (nsets + 1) * 8, cudaMemcpyHostToDevice, ctx->stream);
@@ -708,7 +713,7 @@ static rtg_status si_run(rtg_ctx *ctx, PairSpec &ps, const uint32_t *pair_a,
     double t0 = now_ms();
     uint64_t l0 = ctx->launches;
     uint32_t family = flags & RTG_SI_FAMILY_MASK;
-    if (family > RTG_SI_FORCE_BITMAP)
+    if (family > RTG_SI_PLAIN)
         return fail(ctx, RTG_ERR_INVALID_ARG, "unknown SI family %u", family);
     uint64_t np = ps.npairs;
     uint32_t *d_pa = nullptr, *d_pb = nullptr, *d_out = nullptr;

@@ -17,8 +17,9 @@
 //           n - v - 1 fits the region (high-rank v, which carry almost all of the work on
 //           power-law graphs), else as an open-addressing hash table, else (out-list too long
 //           for the table) it falls back to a tile merge. It then streams the suffixes of the
-//           item's in-edges with coalesced loads, one 128-element block loaded ahead of the
-//           block being tested, and tests every element with one shared-memory load.
+//           item's in-edges as 32-element blocks (one coalesced load per lane), eight blocks
+//           in flight ahead of the one being tested, and tests every element with one
+//           shared-memory load.
 //           Streamed elements: sum over u of d+(u)(d+(u)-1)/2, about a quarter of the
 //           push-order work on power-law graphs. Item build + count are one CUDA graph,
 //           captured once per (graph, schedule) and replayed. uint64 totals: lane partials ->
@@ -39,8 +40,6 @@ namespace {
 constexpr uint32_t kDefaultItemEdges = 256;
 constexpr uint32_t kDefaultBlockWarps = 8;
 constexpr uint32_t kDefaultRegionWords = 1024;   // 4 KB per warp: bitmap of 32,768 ranks
-constexpr uint32_t kDefaultStageSlots = 4;
-constexpr uint32_t kDefaultStageBytes = 1024;
 constexpr uint32_t kPlainRatio = 16;    // long/short above this -> search family (PLAIN)
 constexpr int kPlainBuckets = 6;         // 2 families x 3 size classes
 
@@ -368,18 +367,14 @@ rtg_config effective_config(const rtg_ctx *ctx) {
     rtg_config c = ctx->cfg;
     if (!c.tc_item_edges) c.tc_item_edges = kDefaultItemEdges;
     if (!c.tc_block_warps) c.tc_block_warps = kDefaultBlockWarps;
-    if (!c.tc_stage_slots) c.tc_stage_slots = kDefaultStageSlots;
-    if (!c.tc_stage_bytes) c.tc_stage_bytes = kDefaultStageBytes;
+    if (!c.tc_region_words) c.tc_region_words = kDefaultRegionWords;
     return c;
 }
 
 bool same_tc_config(const rtg_config &a, const rtg_config &b) {
-    return a.tc_item_edges == b.tc_item_edges && a.tc_hash_slots == b.tc_hash_slots &&
-           a.tc_block_warps == b.tc_block_warps && a.tc_blocks_per_sm == b.tc_blocks_per_sm &&
-           a.tc_stage_slots == b.tc_stage_slots && a.tc_stage_bytes == b.tc_stage_bytes;
+    return a.tc_item_edges == b.tc_item_edges && a.tc_region_words == b.tc_region_words &&
+           a.tc_block_warps == b.tc_block_warps && a.tc_blocks_per_sm == b.tc_blocks_per_sm;
 }
-
-inline uint32_t align128(uint32_t x) { return (x + 127u) & ~127u; }
 
 rtg_status batched_plan(rtg_ctx *ctx, rtg_graph *g, TcPlan **out) {
     rtg_config cfg = effective_config(ctx);
@@ -402,7 +397,7 @@ rtg_status batched_plan(rtg_ctx *ctx, rtg_graph *g, TcPlan **out) {
     const uint32_t E = cfg.tc_item_edges, W = cfg.tc_block_warps;
     WarpCfg pc{};
     pc.E = E;
-    pc.R = cfg.tc_hash_slots ? cfg.tc_hash_slots : kDefaultRegionWords;
+    pc.R = cfg.tc_region_words;
     pc.n = c.n;
     const size_t smem = (size_t)W * pc.R * 4;
     if (smem + 256 > (size_t)ctx->smem_optin)

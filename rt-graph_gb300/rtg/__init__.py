@@ -27,7 +27,7 @@ OK, ERR_INVALID_ARG, ERR_OOM, ERR_IO, ERR_FORMAT, ERR_DEVICE, ERR_TIMEOUT, ERR_C
 FMT_EDGE_BIN, FMT_EDGE_TXT, FMT_MTX = 0, 1, 2
 ORIENT_DEGREE, ORIENT_DEGREE_RAW_REF, ORIENT_SYMMETRIC = 0, 1, 2
 TC_PLAIN, TC_BATCHED = 0, 1
-SI_AUTO, SI_MERGE, SI_SEARCH, SI_BITMAP = 0, 1, 2, 3
+SI_AUTO, SI_MERGE, SI_SEARCH, SI_BITMAP, SI_PLAIN = 0, 1, 2, 3, 4
 PAIRS_DEVICE, OUT_DEVICE = 0x100, 0x200
 
 
@@ -51,9 +51,9 @@ class GraphInfo(C.Structure):
 
 class Config(C.Structure):
     _fields_ = [(k, C.c_uint32) for k in (
-        "tc_block_warps", "tc_item_edges", "tc_hash_slots", "tc_blocks_per_sm",
-        "tc_stage_slots", "tc_stage_bytes",
-        "si_block_warps", "si_search_ratio", "si_split_len", "si_pairs_per_grab")]
+        "tc_block_warps", "tc_item_edges", "tc_region_words", "tc_blocks_per_sm",
+        "si_block_warps", "si_search_ratio", "si_stage_slots", "si_stage_bytes",
+        "si_blocks_per_sm")]
 
     def as_dict(self) -> dict:
         return {k: getattr(self, k) for k, _ in self._fields_}

@@ -15,7 +15,7 @@ from conftest import GOLDEN, si_golden, tc_golden, golden_edges
 
 pytestmark = pytest.mark.gpu
 SI = si_golden()
-FAMILIES = (rtg.SI_AUTO, rtg.SI_MERGE, rtg.SI_SEARCH, rtg.SI_BITMAP)
+FAMILIES = (rtg.SI_AUTO, rtg.SI_MERGE, rtg.SI_SEARCH, rtg.SI_BITMAP, rtg.SI_PLAIN)
 
 
 @pytest.mark.parametrize("family", FAMILIES)
@@ -93,6 +93,31 @@ def test_generated_workload_known_answers(ctx, family):
     got, _ = sets.count(pa, pb, family)
     assert np.array_equal(got, exp)
     assert np.array_equal(got, oracle.si_pairs(off, el, pa, pb))
+
+
+@pytest.mark.parametrize("cfg", [
+    dict(si_stage_bytes=512), dict(si_stage_bytes=512, si_stage_slots=2, si_block_warps=1),
+    dict(si_stage_bytes=1024, si_stage_slots=16, si_block_warps=2),
+    dict(si_stage_bytes=32768, si_stage_slots=2, si_block_warps=1), dict(si_blocks_per_sm=1),
+])
+def test_batched_schedules_agree(ctx, cfg):
+    """Small staging slots cut most pairs into many chunk pairs; results must not change."""
+    old = ctx.config()
+    try:
+        ctx.set_config(**cfg)
+        off, el, pa, pb, exp = rtg.gen_si_pairs(20000, seed=9)
+        got, _ = ctx.sets(off, el).count(pa, pb, rtg.SI_AUTO)
+        assert np.array_equal(got, exp)
+        big = np.arange(0, 2 * 65536, 2, dtype=np.uint32)
+        lists = [big, big[::3], big[5:9000], np.array([big[-1]], np.uint32), big + 1]
+        o2 = np.zeros(len(lists) + 1, np.uint64)
+        o2[1:] = np.cumsum([len(x) for x in lists])
+        e2 = np.concatenate(lists).astype(np.uint32)
+        k = len(lists)
+        dense, _ = ctx.sets(o2, e2).count_dense(0, k, 0, k, rtg.SI_AUTO)
+        assert np.array_equal(dense, oracle.si_dense(o2, e2, 0, k, 0, k))
+    finally:
+        ctx.set_config(**old.as_dict())
 
 
 def test_config3_full_size_known_answers(ctx):

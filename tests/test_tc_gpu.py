@@ -77,13 +77,10 @@ def test_cliques_closed_form(ctx, n):
 
 @pytest.mark.parametrize("cfg", [
     dict(tc_item_edges=1), dict(tc_item_edges=7), dict(tc_item_edges=1024),
-    dict(tc_hash_slots=64), dict(tc_hash_slots=256), dict(tc_hash_slots=8192, tc_block_warps=4),
-    dict(tc_block_warps=1),
-    dict(tc_block_warps=16, tc_hash_slots=1024, tc_stage_slots=2, tc_stage_bytes=1024),
-    dict(tc_blocks_per_sm=1),
-    dict(tc_stage_slots=2), dict(tc_stage_slots=16, tc_block_warps=2),
-    dict(tc_stage_bytes=256), dict(tc_stage_bytes=256, tc_stage_slots=3, tc_item_edges=5),
-    dict(tc_stage_bytes=8192, tc_stage_slots=4, tc_block_warps=2),
+    dict(tc_region_words=64), dict(tc_region_words=256),
+    dict(tc_region_words=8192, tc_block_warps=4), dict(tc_region_words=16384, tc_block_warps=2),
+    dict(tc_block_warps=1), dict(tc_block_warps=16, tc_region_words=1024),
+    dict(tc_blocks_per_sm=1), dict(tc_item_edges=3, tc_region_words=128),
 ])
 def test_batched_schedules_agree(ctx, cfg):
     old = ctx.config()
