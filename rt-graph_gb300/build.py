@@ -137,7 +137,8 @@ def build_cli(jobs: int | None = None) -> list[Path]:
         deps = [main_objs[m], *host_objs, LIB]
         if _stale(exe, deps):
             _run([CXX, "-o", str(exe), str(main_objs[m]), *map(str, host_objs),
-                  f"-L{LIBDIR}", "-lrtg", f"-Wl,-rpath,{LIBDIR}", "-fopenmp"])
+                  f"-L{LIBDIR}", "-lrtg", f"-Wl,-rpath,{LIBDIR}", f"-L{CUDA_HOME / 'lib64'}",
+                  "-lcudart", f"-Wl,-rpath,{CUDA_HOME / 'lib64'}", "-fopenmp"])
         out.append(exe)
     return out
 

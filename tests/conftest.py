@@ -23,12 +23,13 @@ GOLDEN = REPO / "tests" / "golden"
 def pytest_configure(config):
     config.addinivalue_line("markers", "gpu: needs a CUDA GPU; calls librtg kernels")
     lib = REPO / "rt-graph_gb300" / "lib" / "librtg.so"
-    if not lib.exists():
+    tools = REPO / "rt-graph_gb300" / "bin" / "s_generator"
+    if not lib.exists() or not tools.exists():
         import importlib.util
         spec = importlib.util.spec_from_file_location("rtg_build", REPO / "rt-graph_gb300" / "build.py")
         mod = importlib.util.module_from_spec(spec)
         spec.loader.exec_module(mod)
-        mod.build_all(cli=False, oracle=True)
+        mod.build_all(cli=True, oracle=True)
 
 
 def tc_golden() -> dict:
