@@ -16,6 +16,12 @@ oriented by degree. A step is one exact uint64 count of the resident CSR:
             (d+(u) + d+(v)) + 8 m) / its CUDA-event duration vs the measured HBM peak.
   cpu_baseline – the oracle's restatement of the reference's ListIntersectionKernel
             (bs_tc.cu:120-148) on the host cores, on a stride sample of source vertices.
+  si      – summary of the batched set-intersection workload (1e6 pairs of sorted unique
+            u32 lists, lengths lognormal with median 64 and sigma 1.5 clamped to [1, 65536],
+            universe [0, 2^26), overlap uniform in [0, 0.5] of the shorter list, seed 1):
+            pairs/s of the persistent staged kernel vs the PLAIN per-pair form, end to end
+            through rtg_si_count, and its roofline. `--workload si` prints that workload
+            alone as a full line (with its CPU baseline).
 
 `--impl reference` runs only the reference's CPU algorithm (oracle port; the reference's
 own code cannot be built on the benchmark host) on the same workload and prints its line.
@@ -44,6 +50,13 @@ WORKLOAD = dict(workload="rmat21_ef16_tc", scale=21, edge_factor=16, abcd=[0.57,
                 seed=42, orientation="degree (post-dedup)", counter="uint64")
 METRIC = "TC edges/s"
 UNIT = "edges/s"
+
+SI_WORKLOAD = dict(workload="si_lognormal_1e6_pairs", npairs=1_000_000, length_median=64,
+                   length_sigma=1.5, length_clamp=[1, 65536], universe="[0, 2^26)",
+                   overlap="uniform [0, 0.5] of the shorter list", seed=1,
+                   storage="CSR (u64 offsets, u32 elements) resident in HBM")
+SI_METRIC = "batched intersections/s"
+SI_UNIT = "pairs/s"
 
 
 def dist_env():
@@ -194,6 +207,164 @@ def cpu_baseline_tc(off: np.ndarray, adj: np.ndarray, target_s: float = 15.0) ->
                       "ListIntersectionKernel restatement (per edge x binary search), OpenMP"}
 
 
+def gen_si_workload():
+    import rtg
+    return rtg.gen_si_pairs(SI_WORKLOAD["npairs"], median=64.0, sigma=1.5, min_len=1,
+                            max_len=65536, universe_log2=26, overlap_max=0.5,
+                            seed=SI_WORKLOAD["seed"])
+
+
+def si_algo_bytes(off: np.ndarray, pa: np.ndarray, pb: np.ndarray) -> int:
+    """4 bytes per element of both lists of every pair + 16 B of pair ids + 4 B of count."""
+    lens = np.diff(off.astype(np.int64))
+    return int(4 * (lens[pa].sum() + lens[pb].sum()) + 20 * len(pa))
+
+
+def cpu_baseline_si(off, el, pa, pb, target_s: float = 10.0) -> dict:
+    """The oracle's per-pair merge (the reference's SerialIntersection, ip.cu:266-287) on a
+    prefix sample of the pairs, split over all host threads."""
+    import oracle
+    threads = os.cpu_count() or 1
+    k = 4096
+    while True:
+        t0 = time.perf_counter()
+        oracle.si_pairs(off, el, pa[:k], pb[:k], threads)
+        dt = time.perf_counter() - t0
+        if dt * 4 > target_s or k >= len(pa):
+            break
+        k = min(len(pa), k * 4)
+    return {"value": k / dt, "unit": SI_UNIT, "cores": threads, "kind": "port",
+            "sample": f"first {k} pairs ({dt:.1f} s), per-pair merge restatement, OpenMP"}
+
+
+def run_reference_si(args, dist: Dist) -> None:
+    if dist.rank != 0:
+        return
+    import oracle
+    off, el, pa, pb, exp = gen_si_workload()
+    threads = os.cpu_count() or 1
+    k = max(1, len(pa) // args.ref_stride)
+    sel = np.arange(0, len(pa), len(pa) // k, dtype=np.int64)[:k]
+    spa, spb = pa[sel], pb[sel]
+    for _ in range(args.warmup):
+        oracle.si_pairs(off, el, spa[: max(1, k // 50)], spb[: max(1, k // 50)], threads)
+    times = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        got = oracle.si_pairs(off, el, spa, spb, threads)
+        times.append(time.perf_counter() - t0)
+    if not np.array_equal(got, exp[sel]):
+        raise RuntimeError("oracle counts differ from the generator's expected counts")
+    ms = 1e3 * sum(times) / len(times)
+    value = k / (ms / 1e3)
+    line = {"metric": SI_METRIC, "value": value, "unit": SI_UNIT, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u32",
+            "data": "synthetic (seeded lognormal pair lists)", "impl": "reference",
+            "config": dict(SI_WORKLOAD, sample_stride=args.ref_stride, sampled_pairs=k),
+            "cpu_baseline": {"value": value, "unit": SI_UNIT, "cores": threads, "kind": "port",
+                             "sample": f"every {args.ref_stride}-th pair, {k} pairs per step; "
+                                       "restatement of the reference's SerialIntersection "
+                                       "(set_intersection/baseline/ip.cu:266-287)"},
+            "e2e": {"value": value, "unit": SI_UNIT, "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def measure_si(args, dist: Dist, ctx, cpu: bool) -> dict:
+    """Batched SI on the 1e6-pair workload: device throughput of the persistent kernel,
+    the PLAIN per-pair form, end-to-end through rtg_si_count with pinned host buffers."""
+    import rtg
+    off, el, pa, pb, exp = gen_si_workload()
+    sets = ctx.sets(off, el)
+    np_ = len(pa)
+    algo = si_algo_bytes(off, pa, pb)
+    for _ in range(args.warmup):
+        ctx.flush_l2()
+        sets.count(pa, pb, rtg.SI_AUTO)
+        sets.count(pa, pb, rtg.SI_PLAIN)
+    l0 = ctx.launches
+    ms_steps, kms_steps = [], []
+    dist.barrier()
+    ctx.sync()
+    with ClockSampler(dist.local) as clk:
+        for _ in range(args.steps):
+            ctx.flush_l2()
+            got, t = sets.count(pa, pb, rtg.SI_AUTO)
+            ms_steps.append(t.count_ms)
+            kms_steps.append(t.main_kernel_ms)
+            if not np.array_equal(got, exp):
+                raise RuntimeError("batched SI counts differ from the expected counts")
+        ctx.sync()
+    dist.barrier()
+    launches = ctx.launches - l0 - args.steps  # flushes are memsets, not kernels
+    value, ms = aggregate(dist, np_, sum(ms_steps) / len(ms_steps))
+    plain_ms = []
+    for _ in range(args.steps):
+        ctx.flush_l2()
+        got, t = sets.count(pa, pb, rtg.SI_PLAIN)
+        plain_ms.append(t.count_ms)
+        if not np.array_equal(got, exp):
+            raise RuntimeError("plain SI counts differ from the expected counts")
+    plain_value, _ = aggregate(dist, np_, sum(plain_ms) / len(plain_ms))
+    hpa = ctx.host_array(np_, np.uint32)
+    hpb = ctx.host_array(np_, np.uint32)
+    hout = ctx.host_array(np_, np.uint32)
+    hpa[:] = pa
+    hpb[:] = pb
+    sets.count(hpa, hpb, rtg.SI_AUTO, out=hout)
+    e2e_ms = []
+    for _ in range(max(1, min(args.steps, 5))):
+        t0 = time.perf_counter()
+        _, te = sets.count(hpa, hpb, rtg.SI_AUTO, out=hout)
+        e2e_ms.append((time.perf_counter() - t0) * 1e3)
+        if not np.array_equal(hout, exp):
+            raise RuntimeError("end-to-end SI counts differ")
+    e2e_value, _ = aggregate(dist, np_, sum(e2e_ms) / len(e2e_ms))
+    kms = sum(kms_steps) / len(kms_steps)
+    peaks = measured_peaks()
+    achieved = algo / (kms / 1e3) / 1e9
+    res = {
+        "value": value, "unit": SI_UNIT, "ms_per_step": ms, "launches": int(launches),
+        "config": dict(SI_WORKLOAD, mode="batched (persistent staged kernel)",
+                       l2="flushed before every step", elements=int(len(el))),
+        "plain": {"value": plain_value, "unit": SI_UNIT,
+                  "ms_per_step": sum(plain_ms) / len(plain_ms)},
+        "batched_over_plain": value / plain_value,
+        "e2e": {"value": e2e_value, "unit": SI_UNIT, "h2d_bytes_per_step": int(te.h2d_bytes),
+                "d2h_bytes_per_step": int(te.d2h_bytes), "ms_per_step": sum(e2e_ms) / len(e2e_ms),
+                "api": "rtg_si_count (pinned host pair ids and counts, sets resident)"},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peaks["hbm_gbs"],
+                     "unit": "GB/s", "frac": achieved / peaks["hbm_gbs"],
+                     "traffic": profile_traffic("si_stream_lognormal_1e6"),
+                     "peak_source": peaks["source"], "kernel": "k_si_stream", "kernel_ms": kms,
+                     "algo_bytes_per_launch": algo},
+        "clocks": clk.summary(),
+        "cpu_baseline": None,
+    }
+    if cpu and dist.rank == 0 and dist.ws == 1:
+        res["cpu_baseline"] = cpu_baseline_si(off, el, pa, pb)
+    sets.close()
+    return res
+
+
+def run_gpu_si(args, dist: Dist) -> None:
+    import rtg
+    ctx = rtg.Context(dist.local if dist.ws > 1 else 0)
+    r = measure_si(args, dist, ctx, cpu=not args.no_cpu_baseline)
+    if dist.rank == 0:
+        line = {"metric": SI_METRIC, "value": r["value"], "unit": SI_UNIT, "n_gpus": dist.ws,
+                "steps": args.steps, "warmup": args.warmup, "ms_per_step": r["ms_per_step"],
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u32",
+                "data": "synthetic (seeded lognormal pair lists, generated on the host)",
+                "config": dict(r["config"], parallelism="replicas" if dist.ws > 1 else "single GPU"),
+                "e2e": r["e2e"], "plain": r["plain"], "batched_over_plain": r["batched_over_plain"],
+                "roofline": r["roofline"], "cpu_baseline": r["cpu_baseline"],
+                "clocks": r["clocks"], "gpu_launches": r["launches"]}
+        print(json.dumps(line), flush=True)
+    ctx.close()
+
+
 def run_reference(args, dist: Dist) -> None:
     if dist.rank != 0:
         return
@@ -297,6 +468,18 @@ def run_gpu(args, dist: Dist) -> None:
     if dist.rank == 0 and dist.ws == 1 and not args.no_cpu_baseline:
         off, adj = g.csr()
         cpu = cpu_baseline_tc(off, adj)
+    g.close()
+    si = None
+    if not args.tc_only:
+        r = measure_si(args, dist, ctx, cpu=False)
+        si = {"metric": SI_METRIC, "value": r["value"], "unit": SI_UNIT,
+              "ms_per_step": r["ms_per_step"], "workload": r["config"]["workload"],
+              "plain": r["plain"], "batched_over_plain": r["batched_over_plain"],
+              "e2e": {k: r["e2e"][k] for k in ("value", "unit", "h2d_bytes_per_step",
+                                               "d2h_bytes_per_step")},
+              "roofline": {k: r["roofline"][k] for k in ("achieved", "peak", "unit", "frac",
+                                                         "traffic", "kernel")},
+              "gpu_launches": r["launches"]}
     if dist.rank == 0:
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": dist.ws,
                 "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
@@ -315,7 +498,7 @@ def run_gpu(args, dist: Dist) -> None:
                           "ms_per_step": sum(plain_ms) / len(plain_ms)},
                 "batched_over_plain": value / plain_value,
                 "roofline": roofline, "cpu_baseline": cpu, "clocks": clk.summary(),
-                "gpu_launches": int(launches)}
+                "gpu_launches": int(launches), "si": si}
         print(json.dumps(line), flush=True)
     ctx.close()
 
@@ -328,15 +511,19 @@ def main() -> None:
     ap.add_argument("--impl", default="rtg", choices=["rtg", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--ref-stride", type=int, default=32)
+    ap.add_argument("--workload", default="tc", choices=["tc", "si"],
+                    help="tc: R-MAT-21 triangle count (with a batched-SI summary); "
+                         "si: the 1e6-pair batched set intersection alone")
+    ap.add_argument("--tc-only", action="store_true", help="skip the batched-SI summary")
     args = ap.parse_args()
     if args.warmup < 3:
         ap.error("at least 3 warm-up steps")
     dist = Dist("gloo" if args.impl == "reference" else None)
     try:
         if args.impl == "reference":
-            run_reference(args, dist)
+            (run_reference_si if args.workload == "si" else run_reference)(args, dist)
         else:
-            run_gpu(args, dist)
+            (run_gpu_si if args.workload == "si" else run_gpu)(args, dist)
     finally:
         dist.close()
 

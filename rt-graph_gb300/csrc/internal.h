@@ -143,8 +143,17 @@ rtg_status tc_count(rtg_ctx *ctx, rtg_graph *g, rtg_tc_mode mode, uint64_t *tota
                     rtg_timing *t);
 void tc_plan_free(TcPlan *p);
 
+// One set collection resident on the device (a symmetric CSR or an rtg_sets).
+struct SetRef {
+    const uint64_t *off;
+    const uint32_t *elems;
+    uint64_t nsets;
+};
+
 // Set intersection (si.cu). Sets are any CSR-like (off, elems); pairs may be implicit
 // dense A x B (dense_nb > 0: pair k = (a_begin + k / dense_nb, b_begin + k % dense_nb)).
+// With gtab set, pair k = (pa[k], pb[k]) of collection gtab[pg[k]] (one launch serving
+// pairs of many collections); off/elems/nsets are then unused.
 struct PairSpec {
     const uint64_t *off = nullptr;
     const uint32_t *elems = nullptr;
@@ -154,6 +163,9 @@ struct PairSpec {
     uint64_t npairs = 0;
     uint32_t dense_nb = 0;
     uint32_t a_begin = 0, b_begin = 0;
+    const uint32_t *pg = nullptr;    // device, with gtab
+    const SetRef *gtab = nullptr;    // device table of ngraphs collections
+    uint32_t ngraphs = 0;
 };
 rtg_status si_count_device(rtg_ctx *ctx, const PairSpec &ps, uint32_t *d_out, uint32_t family,
                            float *kernel_ms, uint64_t *launches);

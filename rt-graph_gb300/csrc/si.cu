@@ -2,14 +2,20 @@
 //
 // BATCHED (RTG_SI_AUTO): one persistent kernel streams every pair through a per-warp ring of
 // shared-memory slots filled by 1-D bulk copies (cp.async.bulk, one mbarrier per slot).
-// A pair whose lists fit one slot is one job. A longer pair is cut into K chunks of each
-// list (K = ceil((|A|+|B|) / slot capacity)); its jobs are the chunk pairs (p, q) whose
-// value ranges overlap, visited in merge order from the chunk maxima (loaded lane-parallel),
-// so every common element lies in exactly one job. Inside a slot every lane takes 1/32 of
-// the merged sequence (merge-path split point by binary search) and merges serially,
-// counting a common element when its B copy is consumed right after an equal A element.
-// Lists are read once from HBM in large asynchronous copies, several jobs in flight per
-// warp.
+// Warps take 32 pairs at a time from an atomic queue and sort each pair into one of:
+//   packed – the pair's two lists fit one slot: consecutive such pairs share a slot (up to
+//            kMaxSeg of them), every lane issuing the copies of its own pair;
+//   chunked – a balanced pair longer than a slot: cut into K chunks of each list
+//            (K = ceil((|A|+|B|) / slot capacity)); its jobs are the chunk pairs (p, q)
+//            whose value ranges overlap, visited in merge order from the chunk maxima, so
+//            every common element lies in exactly one job;
+//   skewed – longer than a slot with |B| > ratio * |A|: the warp binary-searches the short
+//            list's elements in the long list straight from global memory.
+// Inside a slot the merged sequence of all its segments is split evenly over the 32 lanes
+// (merge-path split point by binary search); each lane merges its share serially and counts
+// an element of B when it equals the A element consumed just before it, adding the count of
+// every segment it touched into a per-warp shared counter. Lists are read once from HBM in
+// large asynchronous copies, several slots in flight per warp.
 //
 // Per-family kernel (PLAIN and the forced families): warps take 32 pairs at a time from an
 // atomic queue; lane i loads the ids and list bounds of pair i, then the warp intersects
@@ -51,6 +57,10 @@ struct SiArgs {
     const uint32_t *pb;
     uint64_t np;
     uint32_t dense_nb, a_begin, b_begin;
+    // several collections in one launch: pair k reads collection pg[k] of gtab
+    const uint32_t *pg;
+    const SetRef *gtab;
+    uint32_t ngraphs;
 };
 
 __device__ __forceinline__ bool pair_ids(const SiArgs &s, uint64_t k, uint32_t &x, uint32_t &y) {
@@ -64,35 +74,52 @@ __device__ __forceinline__ bool pair_ids(const SiArgs &s, uint64_t k, uint32_t &
     return x < s.nsets && y < s.nsets;
 }
 
-// Per-lane prefetch of one pair: pointers and lengths, short list first.
+// Per-lane prefetch of one pair: list pointers and lengths, short list first.
 struct PairRef {
-    uint64_t oa, ob;
+    const uint32_t *A, *B;
     uint32_t a, b;
     bool valid;
 };
 
 __device__ __forceinline__ PairRef load_pair(const SiArgs &s, uint64_t k, bool in_range) {
-    PairRef r{0, 0, 0, 0, false};
+    PairRef r{nullptr, nullptr, 0, 0, false};
     if (!in_range) return r;
     uint32_t x, y;
-    if (!pair_ids(s, k, x, y)) return r;
-    uint64_t ox = __ldg(s.off + x), oy = __ldg(s.off + y);
-    uint32_t lx = (uint32_t)(__ldg(s.off + x + 1) - ox), ly = (uint32_t)(__ldg(s.off + y + 1) - oy);
+    const uint64_t *off = s.off;
+    const uint32_t *el = s.elems;
+    if (s.gtab) {
+        const uint32_t g = __ldg(s.pg + k);
+        if (g >= s.ngraphs) return r;
+        const SetRef gr = s.gtab[g];
+        x = __ldg(s.pa + k);
+        y = __ldg(s.pb + k);
+        if (x >= gr.nsets || y >= gr.nsets) return r;
+        off = gr.off;
+        el = gr.elems;
+    } else if (!pair_ids(s, k, x, y)) {
+        return r;
+    }
+    const uint64_t ox = __ldg(off + x), oy = __ldg(off + y);
+    const uint32_t lx = (uint32_t)(__ldg(off + x + 1) - ox), ly = (uint32_t)(__ldg(off + y + 1) - oy);
     if (lx <= ly) {
-        r.oa = ox; r.a = lx; r.ob = oy; r.b = ly;
+        r.A = el + ox; r.a = lx; r.B = el + oy; r.b = ly;
     } else {
-        r.oa = oy; r.a = ly; r.ob = ox; r.b = lx;
+        r.A = el + oy; r.a = ly; r.B = el + ox; r.b = lx;
     }
     r.valid = true;
     return r;
 }
 
-__device__ __forceinline__ uint32_t intersect_family(const uint32_t *elems, uint64_t oa, uint32_t a,
-                                                     uint64_t ob, uint32_t b, uint32_t family,
-                                                     uint32_t ratio, uint32_t *tab, uint32_t H,
-                                                     int lane) {
+__device__ __forceinline__ const uint32_t *shfl_ptr(const uint32_t *p, int src) {
+    return reinterpret_cast<const uint32_t *>(
+        __shfl_sync(kFull, (unsigned long long)reinterpret_cast<uintptr_t>(p), src));
+}
+
+__device__ __forceinline__ uint32_t intersect_family(const uint32_t *A, uint32_t a,
+                                                     const uint32_t *B, uint32_t b,
+                                                     uint32_t family, uint32_t ratio,
+                                                     uint32_t *tab, uint32_t H, int lane) {
     if (a == 0) return 0;
-    const uint32_t *A = elems + oa, *B = elems + ob;
     uint32_t f = family;
     if (f == RTG_SI_PLAIN) f = ((uint64_t)b > (uint64_t)ratio * a) ? RTG_SI_FORCE_SEARCH : RTG_SI_FORCE_MERGE;
     if (f == RTG_SI_FORCE_SEARCH) return warp_search_count(A, a, B, b, lane);
@@ -128,9 +155,9 @@ __global__ void k_si_count(SiArgs s, uint32_t *out, unsigned long long *head, ui
         while (vmask) {
             const int e = __ffs(vmask) - 1;
             vmask &= vmask - 1;
-            const uint64_t oa = __shfl_sync(kFull, r.oa, e), ob = __shfl_sync(kFull, r.ob, e);
+            const uint32_t *A = shfl_ptr(r.A, e), *B = shfl_ptr(r.B, e);
             const uint32_t a = __shfl_sync(kFull, r.a, e), b = __shfl_sync(kFull, r.b, e);
-            uint32_t c = intersect_family(s.elems, oa, a, ob, b, family, ratio, tab, H, lane);
+            uint32_t c = intersect_family(A, a, B, b, family, ratio, tab, H, lane);
             c = __reduce_add_sync(kFull, c);
             if (lane == e) mine = c;
         }
@@ -144,39 +171,50 @@ struct StreamCfg {
     uint32_t S;           // staging slots per warp
     uint32_t slot_words;  // 32-bit words per slot
     uint32_t meta_off;    // byte offsets of the shared-memory regions
+    uint32_t cnt_off;
     uint32_t ring_off;
+    uint32_t ratio;       // a pair longer than a slot is searched when |B| > ratio * |A|
 };
 
-constexpr uint32_t kMetaWords = 8;  // per slot: A offset, |A part|, B offset, |B part|, pair, last
+// Per-slot job description in shared memory (32-bit words):
+//   [0] segments, [1] job kind, [2..3] output index of segment 0's pair (u64), [4] total
+//   merged length L, [kP + s] first diagonal of segment s (kP + nseg holds L),
+//   [kOffA + s] / [kLenA + s] / [kOffB + s] / [kLenB + s] word offset in the slot and length
+//   of the segment's two lists, [kOut + s] output index of segment s relative to [2..3].
+constexpr uint32_t kMaxSeg = 16;
+constexpr uint32_t kP = 8, kOffA = 32, kLenA = 48, kOffB = 64, kLenB = 80, kOut = 96;
+constexpr uint32_t kMetaWords = 112;
+enum : uint32_t { kJobPacked = 0, kJobChunk = 1, kJobChunkLast = 2 };
+enum : uint32_t { kPairZero = 0, kPairPacked = 1, kPairChunked = 2, kPairSkewed = 3 };
 
-// Count |A ∩ B| of two sorted unique lists in shared memory: lane l merges diagonals
-// [l*L/32, (l+1)*L/32) of the merged sequence (ties take A first) and counts an element of
-// B when it equals the A element consumed just before it.
-__device__ __forceinline__ uint32_t merge_path_count(const uint32_t *A, uint32_t na,
-                                                     const uint32_t *B, uint32_t nb, int lane) {
-    const uint32_t L = na + nb;
-    const uint32_t d0 = (uint32_t)(((uint64_t)L * (uint32_t)lane) >> 5);
-    const uint32_t d1 = (uint32_t)(((uint64_t)L * (uint32_t)(lane + 1)) >> 5);
-    uint32_t lo = d0 > nb ? d0 - nb : 0u, hi = min(d0, na);
+// Count the common elements met on diagonals [x0, x1) of the merge of two sorted unique
+// lists in shared memory (ties take A first): a B element is common when it equals the A
+// element consumed just before it. The step is branch-free, one shared load per step.
+__device__ __forceinline__ uint32_t merge_range_count(const uint32_t *A, uint32_t na,
+                                                      const uint32_t *B, uint32_t nb,
+                                                      uint32_t x0, uint32_t x1) {
+    uint32_t lo = x0 > nb ? x0 - nb : 0u, hi = min(x0, na);
     while (lo < hi) {
         const uint32_t mid = (lo + hi) >> 1;
-        if (A[mid] <= B[d0 - 1 - mid]) lo = mid + 1;
+        if (A[mid] <= B[x0 - 1 - mid]) lo = mid + 1;
         else hi = mid;
     }
-    uint32_t i = lo, j = d0 - lo;
+    uint32_t i = lo, j = x0 - lo;
+    // i == 0: every B element consumed before A[0] is smaller than A[0], so the sentinel
+    // never equals one of them
     uint32_t last = i ? A[i - 1] : kEmpty;
-    uint32_t ai = i < na ? A[i] : kEmpty, bj = j < nb ? B[j] : kEmpty;
+    uint32_t ai = A[min(i, na - 1)], bj = B[min(j, nb - 1)];
     uint32_t c = 0;
-    for (uint32_t d = d0; d < d1; ++d) {
-        if (i < na && (j >= nb || ai <= bj)) {
-            last = ai;
-            ++i;
-            ai = i < na ? A[i] : kEmpty;
-        } else {
-            c += (bj == last) ? 1u : 0u;
-            ++j;
-            bj = j < nb ? B[j] : kEmpty;
-        }
+    for (uint32_t d = x0; d < x1; ++d) {
+        const bool ta = i < na && (j >= nb || ai <= bj);
+        c += (!ta && bj == last) ? 1u : 0u;
+        last = ta ? ai : last;
+        i += ta ? 1u : 0u;
+        j += ta ? 0u : 1u;
+        const uint32_t *src = ta ? A + min(i, na - 1) : B + min(j, nb - 1);
+        const uint32_t v = *src;
+        ai = ta ? v : ai;
+        bj = ta ? bj : v;
     }
     return c;
 }
@@ -188,103 +226,201 @@ __global__ void k_si_stream(SiArgs s, uint32_t *out, unsigned long long *head, S
     uint64_t *bars = reinterpret_cast<uint64_t *>(stage_smem) + (size_t)warp * p.S;
     uint32_t *meta =
         reinterpret_cast<uint32_t *>(stage_smem + p.meta_off) + (size_t)warp * p.S * kMetaWords;
+    uint32_t *cnt = reinterpret_cast<uint32_t *>(stage_smem + p.cnt_off) + (size_t)warp * kMaxSeg;
     uint32_t *ring =
         reinterpret_cast<uint32_t *>(stage_smem + p.ring_off) + (size_t)warp * p.S * p.slot_words;
     if ((uint32_t)lane < p.S) mbar_init(bars + lane, 1);
+    if ((uint32_t)lane < kMaxSeg) cnt[lane] = 0;
     fence_mbar_init();
     __syncwarp();
-    const uint32_t CAPE = p.slot_words - 16;  // list elements per job (room for alignment)
+    const uint32_t CAPE = p.slot_words - 16;  // list elements per chunk job (room for alignment)
 
-    // producer: batches of 32 pairs, the next batch fetched one batch ahead
-    auto fetch = [&](unsigned long long &base, PairRef &r) {
+    // One batch of 32 pairs, lane e holding pair base + e: its lists, its kind, the words
+    // its widened lists take in a slot and inclusive warp scans of those words and of the
+    // merged lengths of packed pairs.
+    struct Batch {
+        unsigned long long base;
+        PairRef r;
+        uint32_t kind, w, sw, sl;
+    };
+    auto fetch = [&](Batch &bt) {
         unsigned long long b0 = 0;
         if (lane == 0) b0 = atomicAdd(head, 32ull);
-        base = __shfl_sync(kFull, b0, 0);
-        const uint64_t k = base + lane;
+        bt.base = __shfl_sync(kFull, b0, 0);
+        const uint64_t k = bt.base + lane;
         const bool in = k < s.np;
-        r = load_pair(s, k, in);
-        if (in && !r.valid) {
+        bt.r = load_pair(s, k, in);
+        if (in && !bt.r.valid) {
             atomicExch(status, kStatusBadInput);
             out[k] = 0;
         }
+        bt.kind = kPairZero;
+        bt.w = 0;
+        uint32_t len = 0;
+        if (bt.r.valid && bt.r.a > 0) {
+            const uint32_t hA = (uint32_t)(reinterpret_cast<uintptr_t>(bt.r.A) & 15u) >> 2;
+            const uint32_t hB = (uint32_t)(reinterpret_cast<uintptr_t>(bt.r.B) & 15u) >> 2;
+            const uint64_t ww = (((uint64_t)hA + bt.r.a + 3) & ~3ull) + (((uint64_t)hB + bt.r.b + 3) & ~3ull);
+            if (ww <= p.slot_words) {
+                bt.kind = kPairPacked;
+                bt.w = (uint32_t)ww;
+                len = bt.r.a + bt.r.b;
+            } else if ((uint64_t)bt.r.b > (uint64_t)p.ratio * bt.r.a) {
+                bt.kind = kPairSkewed;
+            } else {
+                bt.kind = kPairChunked;
+            }
+        }
+        bt.sw = bt.w;
+        bt.sl = len;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t x = __shfl_up_sync(kFull, bt.sw, o), y = __shfl_up_sync(kFull, bt.sl, o);
+            if (lane >= o) {
+                bt.sw += x;
+                bt.sl += y;
+            }
+        }
     };
-    unsigned long long cb, nb;
-    PairRef cr, nr;
-    fetch(cb, cr);
-    fetch(nb, nr);
+    Batch cur, nxt;
+    fetch(cur);
+    fetch(nxt);
     uint32_t e = 0;
-    // the pair being cut into jobs (warp-uniform)
+    // the chunked pair being cut into jobs (warp-uniform)
     bool open = false;
-    uint64_t oa = 0, ob = 0, pk = 0;
+    const uint32_t *LA = nullptr, *LB = nullptr;  // the pair's short and long list
+    uint64_t pk = 0;
     uint32_t a = 0, b = 0, CA = 0, CB = 0, KA = 0, KB = 0, pA = 0, qB = 0, wA = 0, wB = 0;
     uint32_t mxA = kEmpty, mxB = kEmpty;  // lane t: largest element of chunk wA+t / wB+t
-    auto chunk_max = [&](uint32_t w, uint32_t K, uint32_t C, uint64_t o, uint32_t len) {
+    auto chunk_max = [&](uint32_t w, uint32_t K, uint32_t C, const uint32_t *L, uint32_t len) {
         const uint32_t t = w + lane;
-        return t < K ? __ldg(s.elems + o + min((t + 1) * C, len) - 1) : kEmpty;
+        return t < K ? __ldg(L + min((t + 1) * C, len) - 1) : kEmpty;
     };
-    auto next_job = [&](uint32_t &a0, uint32_t &na, uint32_t &b0, uint32_t &nbb, bool &last) {
+
+    // Fill slot `slot` (meta `mt`, barrier `bar`) with the next job; false when none is left.
+    auto issue_job = [&](uint32_t *slot, uint32_t *mt, uint64_t *bar) -> bool {
         while (!open) {
-            if (cb >= s.np) return false;
-            if (e >= 32 || cb + e >= s.np) {
-                cb = nb;
-                cr = nr;
+            if (cur.base >= s.np) return false;
+            const uint32_t nbat = (s.np - cur.base < 32ull) ? (uint32_t)(s.np - cur.base) : 32u;
+            if (e >= nbat) {
+                cur = nxt;
                 e = 0;
-                if (cb < s.np) fetch(nb, nr);
+                if (cur.base < s.np) fetch(nxt);
                 continue;
             }
-            const bool valid = __shfl_sync(kFull, cr.valid ? 1u : 0u, e) != 0u;
-            oa = __shfl_sync(kFull, cr.oa, e);
-            ob = __shfl_sync(kFull, cr.ob, e);
-            a = __shfl_sync(kFull, cr.a, e);
-            b = __shfl_sync(kFull, cr.b, e);
-            pk = cb + e;
+            const uint32_t kind = __shfl_sync(kFull, cur.kind, e);
+            if (kind == kPairZero || kind == kPairPacked) {
+                // consecutive packed (and empty) pairs e .. e1-1 that fit one slot together
+                const uint32_t baseW = e ? __shfl_sync(kFull, cur.sw, e - 1) : 0u;
+                const uint32_t baseL = e ? __shfl_sync(kFull, cur.sl, e - 1) : 0u;
+                const uint32_t me = (uint32_t)lane;
+                const bool brk = me > e && (me >= nbat || cur.kind == kPairChunked ||
+                                            cur.kind == kPairSkewed || cur.sw - baseW > p.slot_words ||
+                                            me >= e + kMaxSeg);
+                const unsigned bm = __ballot_sync(kFull, brk);
+                const uint32_t e1 = bm ? (uint32_t)(__ffs(bm) - 1) : 32u;
+                const uint32_t nseg = e1 - e;
+                const uint32_t totW = __shfl_sync(kFull, cur.sw, e1 - 1) - baseW;
+                const uint32_t L = __shfl_sync(kFull, cur.sl, e1 - 1) - baseL;
+                const bool mine = me >= e && me < e1;
+                uint32_t dst = 0, hA = 0, hB = 0, wa = 0;
+                if (mine) {
+                    const uint32_t sg = me - e;
+                    dst = cur.sw - cur.w - baseW;
+                    const bool pk_ = cur.kind == kPairPacked;
+                    hA = (uint32_t)(reinterpret_cast<uintptr_t>(cur.r.A) & 15u) >> 2;
+                    hB = (uint32_t)(reinterpret_cast<uintptr_t>(cur.r.B) & 15u) >> 2;
+                    wa = (hA + cur.r.a + 3) & ~3u;
+                    mt[kP + sg] = cur.sl - (pk_ ? cur.r.a + cur.r.b : 0u) - baseL;
+                    mt[kOffA + sg] = dst + hA;
+                    mt[kLenA + sg] = pk_ ? cur.r.a : 0u;
+                    mt[kOffB + sg] = dst + wa + hB;
+                    mt[kLenB + sg] = pk_ ? cur.r.b : 0u;
+                    mt[kOut + sg] = me;
+                }
+                if (lane == 0) {
+                    mt[0] = nseg;
+                    mt[1] = kJobPacked;
+                    mt[2] = (uint32_t)cur.base;
+                    mt[3] = (uint32_t)(cur.base >> 32);
+                    mt[4] = L;
+                    mt[kP + nseg] = L;
+                    mbar_arrive_expect_tx(bar, totW * 4u);
+                }
+                __syncwarp();
+                if (mine && cur.kind == kPairPacked) {
+                    const uintptr_t gaa = reinterpret_cast<uintptr_t>(cur.r.A) & ~(uintptr_t)15;
+                    const uintptr_t gbb = reinterpret_cast<uintptr_t>(cur.r.B) & ~(uintptr_t)15;
+                    bulk_copy_g2s(slot + dst, reinterpret_cast<const void *>(gaa), wa * 4u, bar);
+                    bulk_copy_g2s(slot + dst + wa, reinterpret_cast<const void *>(gbb),
+                                  (cur.w - wa) * 4u, bar);
+                }
+                e = e1;
+                return true;
+            }
+            LA = shfl_ptr(cur.r.A, e);
+            LB = shfl_ptr(cur.r.B, e);
+            a = __shfl_sync(kFull, cur.r.a, e);
+            b = __shfl_sync(kFull, cur.r.b, e);
+            pk = cur.base + e;
             ++e;
-            if (!valid) continue;
-            if (a == 0) {  // a <= b: an empty list meets nothing
-                if (lane == 0) out[pk] = 0;
+            if (kind == kPairSkewed) {
+                uint32_t c = warp_search_count(LA, a, LB, b, lane);
+                c = __reduce_add_sync(kFull, c);
+                if (lane == 0) out[pk] = c;
                 continue;
             }
-            if ((uint64_t)a + b <= CAPE) {
-                CA = a;
-                CB = b;
-                KA = KB = 1;
-            } else {
-                const uint32_t K = (uint32_t)(((uint64_t)a + b + CAPE - 1) / CAPE);
-                CA = (a + K - 1) / K;
-                CB = (b + K - 1) / K;
-                KA = (a + CA - 1) / CA;
-                KB = (b + CB - 1) / CB;
-                mxA = chunk_max(0, KA, CA, oa, a);
-                mxB = chunk_max(0, KB, CB, ob, b);
-            }
+            const uint32_t K = (uint32_t)(((uint64_t)a + b + CAPE - 1) / CAPE);
+            CA = (a + K - 1) / K;
+            CB = (b + K - 1) / K;
+            KA = (a + CA - 1) / CA;
+            KB = (b + CB - 1) / CB;
+            mxA = chunk_max(0, KA, CA, LA, a);
+            mxB = chunk_max(0, KB, CB, LB, b);
             pA = qB = wA = wB = 0;
             open = true;
         }
-        a0 = pA * CA;
-        na = min(CA, a - a0);
-        b0 = qB * CB;
-        nbb = min(CB, b - b0);
-        if (KA == 1 && KB == 1) {
-            last = true;
-            open = false;
-            return true;
-        }
-        // next chunk pair in merge order of the chunk maxima
+        // next chunk pair of the open pair, in merge order of the chunk maxima
+        const uint32_t a0 = pA * CA, na = min(CA, a - a0);
+        const uint32_t b0 = qB * CB, nbb = min(CB, b - b0);
         const uint32_t ma = __shfl_sync(kFull, mxA, pA - wA), mb = __shfl_sync(kFull, mxB, qB - wB);
         if (ma <= mb) ++pA;
         if (mb <= ma) ++qB;
-        last = pA >= KA || qB >= KB;
+        const bool last = pA >= KA || qB >= KB;
         if (last) {
             open = false;
         } else {
             if (pA - wA >= 32) {
                 wA += 32;
-                mxA = chunk_max(wA, KA, CA, oa, a);
+                mxA = chunk_max(wA, KA, CA, LA, a);
             }
             if (qB - wB >= 32) {
                 wB += 32;
-                mxB = chunk_max(wB, KB, CB, ob, b);
+                mxB = chunk_max(wB, KB, CB, LB, b);
             }
+        }
+        if (lane == 0) {
+            const uintptr_t ga = reinterpret_cast<uintptr_t>(LA + a0);
+            const uintptr_t gb = reinterpret_cast<uintptr_t>(LB + b0);
+            const uintptr_t gaa = ga & ~(uintptr_t)15, gbb = gb & ~(uintptr_t)15;
+            const uint32_t hA = (uint32_t)(ga - gaa) >> 2, hB = (uint32_t)(gb - gbb) >> 2;
+            const uint32_t bytesA = ((hA + na) * 4u + 15u) & ~15u;
+            const uint32_t bytesB = ((hB + nbb) * 4u + 15u) & ~15u;
+            mt[0] = 1;
+            mt[1] = last ? kJobChunkLast : kJobChunk;
+            mt[2] = (uint32_t)pk;
+            mt[3] = (uint32_t)(pk >> 32);
+            mt[4] = na + nbb;
+            mt[kP] = 0;
+            mt[kP + 1] = na + nbb;
+            mt[kOffA] = hA;
+            mt[kLenA] = na;
+            mt[kOffB] = bytesA / 4 + hB;
+            mt[kLenB] = nbb;
+            mt[kOut] = 0;
+            mbar_arrive_expect_tx(bar, bytesA + bytesB);
+            bulk_copy_g2s(slot, reinterpret_cast<const void *>(gaa), bytesA, bar);
+            bulk_copy_g2s(slot + bytesA / 4, reinterpret_cast<const void *>(gbb), bytesB, bar);
         }
         return true;
     };
@@ -293,31 +429,9 @@ __global__ void k_si_stream(SiArgs s, uint32_t *out, unsigned long long *head, S
     bool jobs = true;
     while (true) {
         while (inflight < p.S && jobs) {
-            uint32_t a0, na, b0, nbb;
-            bool last;
-            if (!next_job(a0, na, b0, nbb, last)) {
+            if (!issue_job(ring + (size_t)sw * p.slot_words, meta + sw * kMetaWords, bars + sw)) {
                 jobs = false;
                 break;
-            }
-            const uintptr_t ga = reinterpret_cast<uintptr_t>(s.elems + oa + a0);
-            const uintptr_t gb = reinterpret_cast<uintptr_t>(s.elems + ob + b0);
-            const uintptr_t gaa = ga & ~(uintptr_t)15, gbb = gb & ~(uintptr_t)15;
-            const uint32_t hA = (uint32_t)(ga - gaa) >> 2, hB = (uint32_t)(gb - gbb) >> 2;
-            const uint32_t bytesA = ((hA + na) * 4u + 15u) & ~15u;
-            const uint32_t bytesB = ((hB + nbb) * 4u + 15u) & ~15u;
-            uint32_t *slot = ring + (size_t)sw * p.slot_words;
-            if (lane == 0) {
-                uint32_t *mt = meta + sw * kMetaWords;
-                mt[0] = hA;
-                mt[1] = na;
-                mt[2] = bytesA / 4 + hB;
-                mt[3] = nbb;
-                mt[4] = (uint32_t)pk;
-                mt[5] = last ? 1u : 0u;
-                mbar_arrive_expect_tx(bars + sw, bytesA + bytesB);
-                bulk_copy_g2s(slot, reinterpret_cast<const void *>(gaa), bytesA, bars + sw);
-                bulk_copy_g2s(slot + bytesA / 4, reinterpret_cast<const void *>(gbb), bytesB,
-                              bars + sw);
             }
             sw = (sw + 1 == p.S) ? 0 : sw + 1;
             ++inflight;
@@ -335,12 +449,41 @@ __global__ void k_si_stream(SiArgs s, uint32_t *out, unsigned long long *head, S
         phase ^= 1u << sr;
         const uint32_t *mt = meta + sr * kMetaWords;
         const uint32_t *slot = ring + (size_t)sr * p.slot_words;
-        uint32_t c = merge_path_count(slot + mt[0], mt[1], slot + mt[2], mt[3], lane);
-        c = __reduce_add_sync(kFull, c);
-        acc += c;
-        if (mt[5]) {
-            if (lane == 0) out[mt[4]] = acc;
-            acc = 0;
+        const uint32_t nseg = mt[0], kind = mt[1], L = mt[4];
+        uint32_t d0 = (uint32_t)(((uint64_t)L * (uint32_t)lane) >> 5);
+        const uint32_t d1 = (uint32_t)(((uint64_t)L * (uint32_t)(lane + 1)) >> 5);
+        if (d0 < d1) {
+            // last segment starting at or before d0 (P is non-decreasing, P[nseg] = L > d0)
+            uint32_t sg = 0;
+#pragma unroll
+            for (uint32_t st = kMaxSeg / 2; st; st >>= 1)
+                if (sg + st < nseg && mt[kP + sg + st] <= d0) sg += st;
+            while (d0 < d1) {
+                const uint32_t ps = mt[kP + sg], pe = mt[kP + sg + 1];
+                const uint32_t x1 = min(d1, pe) - ps;
+                const uint32_t c = merge_range_count(slot + mt[kOffA + sg], mt[kLenA + sg],
+                                                     slot + mt[kOffB + sg], mt[kLenB + sg],
+                                                     d0 - ps, x1);
+                if (c) atomicAdd(cnt + sg, c);
+                d0 = ps + x1;
+                ++sg;
+                while (d0 < d1 && mt[kP + sg + 1] <= d0) ++sg;  // skip empty segments
+            }
+        }
+        __syncwarp();
+        const uint64_t obase = (uint64_t)mt[2] | ((uint64_t)mt[3] << 32);
+        if (kind == kJobPacked) {
+            if ((uint32_t)lane < nseg) {
+                out[obase + mt[kOut + lane]] = cnt[lane];
+                cnt[lane] = 0;
+            }
+        } else if (lane == 0) {
+            acc += cnt[0];
+            cnt[0] = 0;
+            if (kind == kJobChunkLast) {
+                out[obase] = acc;
+                acc = 0;
+            }
         }
         __syncwarp();
         fence_proxy_async_smem();
@@ -379,6 +522,9 @@ SiArgs make_args(const PairSpec &ps) {
     a.dense_nb = ps.dense_nb;
     a.a_begin = ps.a_begin;
     a.b_begin = ps.b_begin;
+    a.pg = ps.pg;
+    a.gtab = ps.gtab;
+    a.ngraphs = ps.ngraphs;
     return a;
 }
 
@@ -390,15 +536,18 @@ rtg_status si_count_device(rtg_ctx *ctx, const PairSpec &ps, uint32_t *d_out, ui
         if (kernel_ms) *kernel_ms = 0;
         return RTG_OK;
     }
+    const rtg_config &cf = ctx->cfg;
+    const uint32_t ratio = cf.si_search_ratio ? cf.si_search_ratio : kDefaultSearchRatio;
     if (family == RTG_SI_AUTO) {
-        const rtg_config &cf = ctx->cfg;
         const uint32_t W = cf.si_block_warps ? cf.si_block_warps : kDefaultStreamWarps;
         StreamCfg sc{};
         sc.S = cf.si_stage_slots ? cf.si_stage_slots : kDefaultStageSlots;
         const uint32_t slot_bytes = cf.si_stage_bytes ? cf.si_stage_bytes : kDefaultStageBytes;
         sc.slot_words = slot_bytes / 4;
+        sc.ratio = ratio;
         sc.meta_off = ((W * sc.S * 8) + 127u) & ~127u;
-        sc.ring_off = (sc.meta_off + W * sc.S * kMetaWords * 4 + 127u) & ~127u;
+        sc.cnt_off = (sc.meta_off + W * sc.S * kMetaWords * 4 + 127u) & ~127u;
+        sc.ring_off = (sc.cnt_off + W * kMaxSeg * 4 + 127u) & ~127u;
         const size_t smem = (size_t)sc.ring_off + (size_t)W * sc.S * slot_bytes;
         if ((int)smem > ctx->smem_optin)
             return fail(ctx, RTG_ERR_INVALID_ARG, "SI schedule needs %zu B of shared memory", smem);
@@ -424,8 +573,7 @@ rtg_status si_count_device(rtg_ctx *ctx, const PairSpec &ps, uint32_t *d_out, ui
         }
         return RTG_OK;
     }
-    const uint32_t W = ctx->cfg.si_block_warps ? ctx->cfg.si_block_warps : kDefaultSiWarps;
-    const uint32_t ratio = ctx->cfg.si_search_ratio ? ctx->cfg.si_search_ratio : kDefaultSearchRatio;
+    const uint32_t W = cf.si_block_warps ? cf.si_block_warps : kDefaultSiWarps;
     const uint32_t H = (family == RTG_SI_FORCE_BITMAP) ? kSiHashSlots : 0;
     const size_t smem = (size_t)W * H * 4;
     if ((int)smem > ctx->smem_optin)

@@ -462,10 +462,15 @@ class Sets:
     def nsets(self) -> int:
         return lib.rtg_sets_count(self.h)
 
-    def count(self, pa: np.ndarray, pb: np.ndarray, family: int = SI_AUTO):
+    def count(self, pa: np.ndarray, pb: np.ndarray, family: int = SI_AUTO,
+              out: np.ndarray | None = None):
+        """Per-pair intersection sizes; `out` (uint32, len(pa)) may be a pinned host array."""
         pa = np.ascontiguousarray(pa, np.uint32)
         pb = np.ascontiguousarray(pb, np.uint32)
-        out = np.empty(max(len(pa), 1), np.uint32)
+        if out is None:
+            out = np.empty(max(len(pa), 1), np.uint32)
+        elif out.dtype != np.uint32 or not out.flags.c_contiguous or len(out) < len(pa):
+            raise ValueError("out must be a contiguous uint32 array of len(pa) elements")
         t = Timing()
         self.ctx.check(lib.rtg_si_count(self.ctx.h, self.h, _ptr(pa), _ptr(pb), len(pa),
                                         _ptr(out), family, C.byref(t)), "si_count")
