@@ -117,7 +117,7 @@ class ClockSampler:
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}",
-                 "--format=csv,noheader,nounits", "-lms", "200"],
+                 "--format=csv,noheader,nounits", "-lms", "50"],
                 stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.t = threading.Thread(target=self._read, daemon=True)
             self.t.start()
@@ -297,7 +297,7 @@ def measure_si(args, dist: Dist, ctx, cpu: bool) -> dict:
                 raise RuntimeError("batched SI counts differ from the expected counts")
         ctx.sync()
     dist.barrier()
-    launches = ctx.launches - l0 - args.steps  # flushes are memsets, not kernels
+    launches = ctx.launches - l0  # kernels only: the L2 flush is a memset
     value, ms = aggregate(dist, np_, sum(ms_steps) / len(ms_steps))
     plain_ms = []
     for _ in range(args.steps):
@@ -430,7 +430,7 @@ def run_gpu(args, dist: Dist) -> None:
             kms_steps.append(t.main_kernel_ms)
         ctx.sync()
     dist.barrier()
-    launches = ctx.launches - launches0 - args.steps  # flushes are memsets, not kernels
+    launches = ctx.launches - launches0  # kernels only: the L2 flush is a memset
     algo_bytes = t.algo_bytes
     ms_local = sum(ms_steps) / len(ms_steps)
     value, ms = aggregate(dist, m, ms_local)
@@ -506,7 +506,7 @@ def run_gpu(args, dist: Dist) -> None:
 def main() -> None:
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--steps", type=int, default=30)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="rtg", choices=["rtg", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")

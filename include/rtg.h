@@ -277,6 +277,105 @@ rtg_status rtg_si_materialize(rtg_ctx *ctx, const rtg_sets *s, const uint32_t *p
                               const uint32_t *pair_b, uint64_t npairs, uint64_t *out_offsets,
                               uint32_t *out_elems, uint64_t out_capacity, rtg_timing *timing);
 
+/* ----------------------------------------------------------------- serving
+ * A request loop over many graphs resident in HBM. No counterpart in the reference,
+ * whose mains run one graph or one dataset per process; it serves the reference's two
+ * computations as requests: the triangle count of a graph (what CountOnGPU prints,
+ * tc/bs_tc/bs_tc.cu:232-354) and intersection counts |N(u) ∩ N(v)| of vertex pairs on a
+ * graph's symmetric adjacency (the per-pair count of the SI baselines).
+ *
+ * rtg_serve_start creates the server and its engine thread on one device. Graphs are
+ * built on the GPU from host edges (the symmetric CSR for pair queries and the oriented
+ * counting form for triangle counts) and stay resident until removed. Submissions are
+ * thread-safe and return at once with a request id. The engine admits work against the
+ * HBM budget; packs the pair requests waiting at each launch point, of any graphs and any
+ * sizes, into one persistent set-intersection launch (up to si_slots launches in flight
+ * on their own streams); runs triangle counts as CUDA-graph replays on another stream, so
+ * both kinds overlap on the device; coalesces triangle-count requests of one graph that
+ * wait together; and completes requests as their launches finish.
+ *
+ * Borrowed buffers: the pair arrays u, v and the output out_counts of
+ * rtg_serve_submit_pairs are read and written by the engine after the call returns; they
+ * must stay valid until the request is reported complete (rtg_serve_poll or
+ * rtg_serve_wait_any returned it) or rtg_serve_stop returned. */
+typedef struct rtg_server rtg_server;
+
+typedef struct rtg_serve_config {
+    uint64_t hbm_budget_bytes; /* resident graphs + counting plans + launch buffers;
+                                  0 = 90% of the free device memory at start            */
+    uint32_t max_batch_pairs;  /* pairs per set-intersection launch (default 1 << 19)   */
+    uint32_t si_slots;         /* set-intersection launches in flight (default 2; 1..4) */
+    uint32_t max_graphs;       /* resident graph slots (default 1024)                   */
+    uint32_t flags;            /* RTG_SERVE_*                                           */
+    uint32_t inject_fail_launch; /* testing: the n-th set-intersection launch (1-based)
+                                    is reported failed on the host, as if its completion
+                                    query had returned an error (0 = off)              */
+    uint32_t reserved;
+} rtg_serve_config;
+
+/* The engine launches nothing until rtg_serve_release (deterministic tests). */
+#define RTG_SERVE_START_HELD 0x1u
+
+typedef enum rtg_request_kind { RTG_REQ_TC = 0, RTG_REQ_PAIRS = 1 } rtg_request_kind;
+
+typedef struct rtg_request_info {
+    rtg_status status;       /* OK, CANCELLED, DEVICE, TIMEOUT, OOM                      */
+    uint32_t kind;           /* rtg_request_kind                                          */
+    uint32_t graph;
+    uint32_t launches;       /* launches the request took part in                        */
+    uint32_t batch_requests; /* most requests that shared one of those launches          */
+    uint32_t reserved;
+    uint64_t npairs;
+    uint64_t triangles;      /* RTG_REQ_TC                                                */
+    double latency_ms;       /* submission -> completion                                 */
+    double queue_ms;         /* submission -> first launch                               */
+} rtg_request_info;
+
+typedef struct rtg_serve_stats {
+    uint64_t submitted, completed, failed, cancelled;
+    uint64_t tc_launches, tc_coalesced;   /* TC requests served by another's launch      */
+    uint64_t si_launches, si_pairs, max_requests_per_launch;
+    uint64_t max_inflight_launches;       /* TC + SI launches in flight at one time      */
+    uint64_t resident_graphs, resident_bytes, plan_bytes, buffer_bytes, budget_bytes;
+    uint64_t plan_evictions, admission_waits;
+} rtg_serve_stats;
+
+rtg_status rtg_serve_start(int device, const rtg_serve_config *cfg, rtg_server **out);
+/* Cancels queued requests, waits for launches in flight, frees every graph. */
+void rtg_serve_stop(rtg_server *s);
+const char *rtg_serve_last_error(const rtg_server *s);
+/* Build a resident graph from host edges (copied). RTG_ERR_OOM when it does not fit the
+ * budget, RTG_ERR_BUSY when every graph slot is taken. */
+rtg_status rtg_serve_add_graph(rtg_server *s, const uint32_t *src, const uint32_t *dst,
+                               uint64_t m, uint32_t *graph_id);
+rtg_status rtg_serve_add_graph_file(rtg_server *s, const char *path, rtg_format fmt,
+                                    uint32_t *graph_id);
+/* New requests on the graph are refused at once; it is freed when its last queued or
+ * running request completes. */
+rtg_status rtg_serve_remove_graph(rtg_server *s, uint32_t graph_id);
+rtg_status rtg_serve_graph_info(rtg_server *s, uint32_t graph_id, rtg_graph_info *info);
+rtg_status rtg_serve_submit_tc(rtg_server *s, uint32_t graph_id, uint64_t *request_id);
+/* Vertex ids must be below the graph's n_sym (checked here: RTG_ERR_INVALID_ARG). */
+rtg_status rtg_serve_submit_pairs(rtg_server *s, uint32_t graph_id, const uint32_t *u,
+                                  const uint32_t *v, uint64_t npairs, uint32_t *out_counts,
+                                  uint64_t *request_id);
+/* wait_ms: 0 polls, < 0 waits without limit. RTG_OK with *info once the request is
+ * complete (the id is then forgotten); RTG_ERR_BUSY while it is not; RTG_ERR_INVALID_ARG
+ * for an unknown id. */
+rtg_status rtg_serve_poll(rtg_server *s, uint64_t request_id, int32_t wait_ms,
+                          rtg_request_info *info);
+/* The next completed request not yet collected, in completion order. */
+rtg_status rtg_serve_wait_any(rtg_server *s, int32_t wait_ms, uint64_t *request_id,
+                              rtg_request_info *info);
+/* A queued request completes at once as RTG_ERR_CANCELLED; a running one stops taking
+ * new launches, its results are discarded, and it completes as RTG_ERR_CANCELLED when
+ * its launches in flight finish. */
+rtg_status rtg_serve_cancel(rtg_server *s, uint64_t request_id);
+rtg_status rtg_serve_release(rtg_server *s);
+/* Wait until no request is queued or running (wait_ms as for rtg_serve_poll). */
+rtg_status rtg_serve_drain(rtg_server *s, int32_t wait_ms);
+rtg_status rtg_serve_stats_get(rtg_server *s, rtg_serve_stats *st);
+
 /* --------------------------------------------------------- dataset files */
 /* Reference .s_data/.m_data header (set_intersection/utils/util.cpp:3-23 and
  * data_generator/data.cpp:344-373). */

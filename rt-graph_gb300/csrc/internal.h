@@ -142,6 +142,14 @@ void count_csr_free(CountCsr &cc);
 rtg_status tc_count(rtg_ctx *ctx, rtg_graph *g, rtg_tc_mode mode, uint64_t *total,
                     rtg_timing *t);
 void tc_plan_free(TcPlan *p);
+// Serving: enqueue the batched count of g (building its plan on first use) on ctx's
+// stream without waiting; the total lands in the pinned host word *h_total when the
+// stream reaches it. At most one such count of a graph may be in flight.
+rtg_status tc_launch_async(rtg_ctx *ctx, rtg_graph *g, unsigned long long *h_total);
+// Device bytes the batched plan of g will hold (upper estimate).
+uint64_t tc_plan_estimate_bytes(const rtg_ctx *ctx, const rtg_graph *g);
+// Free the batched plan of g (no count of g may be in flight).
+void tc_plan_release(rtg_graph *g);
 
 // One set collection resident on the device (a symmetric CSR or an rtg_sets).
 struct SetRef {

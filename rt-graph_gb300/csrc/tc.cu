@@ -572,6 +572,35 @@ rtg_status count_plain(rtg_ctx *ctx, rtg_graph *g, uint64_t *total, rtg_timing *
 
 }  // namespace
 
+uint64_t tc_plan_estimate_bytes(const rtg_ctx *ctx, const rtg_graph *g) {
+    const rtg_config cfg = effective_config(ctx);
+    const CountCsr &c = g->cnt;
+    // items + vertex counts + scan temporary (bounded by one word per vertex) + totals
+    return (c.m / cfg.tc_item_edges + c.n + 1) * 8 + (c.n + 1ull) * 8 + (c.n + 1ull) * 4 + 4096;
+}
+
+rtg_status tc_launch_async(rtg_ctx *ctx, rtg_graph *g, unsigned long long *h_total) {
+    const CountCsr &c = g->cnt;
+    if (!c.built) return fail(ctx, RTG_ERR_STATE, "counting form of the CSR is missing");
+    if (c.n > 0x7FFFFFFFu || c.m >= (1ull << 32))
+        return fail(ctx, RTG_ERR_INVALID_ARG, "graph too large for 32-bit edge ids");
+    if (c.m == 0) {
+        *h_total = 0;
+        return RTG_OK;
+    }
+    TcPlan *p = nullptr;
+    RTG_TRY(batched_plan(ctx, g, &p));
+    RTG_CUDA(ctx, cudaGraphLaunch(p->exec, ctx->stream));
+    ctx->launches += p->graph_kernels;
+    RTG_CUDA(ctx, cudaMemcpyAsync(h_total, p->acc, 8, cudaMemcpyDeviceToHost, ctx->stream));
+    return RTG_OK;
+}
+
+void tc_plan_release(rtg_graph *g) {
+    tc_plan_free(g->plan_batched);
+    g->plan_batched = nullptr;
+}
+
 rtg_status tc_count(rtg_ctx *ctx, rtg_graph *g, rtg_tc_mode mode, uint64_t *total,
                     rtg_timing *t) {
     const Csr &c = g->ori;
