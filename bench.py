@@ -365,6 +365,143 @@ def run_gpu_si(args, dist: Dist) -> None:
     ctx.close()
 
 
+SERVE_WORKLOAD = dict(workload="serve_rmat14to20_x64", graphs=64, scales=[14, 20],
+                      edge_factor=16, abcd=[0.57, 0.19, 0.19, 0.05], requests=10_000,
+                      p_tc=0.2, pairs_per_request=[1000, 100_000], arrivals="Poisson",
+                      load_levels=[0.5, 0.8, 0.95], seed=5,
+                      pair_query="|N(u) ∩ N(v)| on the symmetric adjacency, u, v uniform")
+
+
+def serve_setup(seed: int):
+    """64 seeded R-MAT graphs (scales uniform over 14..20) and per-graph pools of random
+    vertex pairs; requests take windows of a pool."""
+    import rtg
+    rng = np.random.default_rng(seed)
+    scales = rng.integers(14, 21, SERVE_WORKLOAD["graphs"])
+    graphs = []
+    for i, sc in enumerate(scales):
+        s, d = rtg.gen_rmat(int(sc), 16, 0.57, 0.19, 0.19, seed=1000 + i)
+        graphs.append((int(sc), s, d))
+    return graphs
+
+
+def serve_requests(rng, ngraphs: int, n_sym: list[int], count: int, pools):
+    lo, hi = SERVE_WORKLOAD["pairs_per_request"]
+    reqs = []
+    for _ in range(count):
+        g = int(rng.integers(ngraphs))
+        if rng.random() < SERVE_WORKLOAD["p_tc"]:
+            reqs.append((g, 0, 0))
+        else:
+            k = int(rng.integers(lo, hi + 1))
+            o = int(rng.integers(0, len(pools[g][0]) - k + 1))
+            reqs.append((g, o, k))
+    return reqs
+
+
+def serve_run(srv, gids, pools, reqs, rate: float | None, m_of: list[int]) -> dict:
+    """Submit `reqs` (all at once when rate is None, else Poisson arrivals at `rate`
+    requests/s) from one thread while another collects completions."""
+    done: list[dict] = []
+    n = len(reqs)
+
+    def collect():
+        while len(done) < n:
+            r = srv.wait_any(1000)
+            if r is not None:
+                done.append(r[1])
+
+    col = threading.Thread(target=collect, daemon=True)
+    rng = np.random.default_rng(17)
+    gaps = rng.exponential(1.0 / rate, n) if rate else np.zeros(n)
+    col.start()
+    t0 = time.perf_counter()
+    due = t0
+    for (g, o, k), gap in zip(reqs, gaps):
+        due += gap
+        while True:
+            now = time.perf_counter()
+            if now >= due:
+                break
+            time.sleep(min(due - now, 0.0005))
+        if k == 0:
+            srv.submit_tc(gids[g])
+        else:
+            u, v = pools[g]
+            srv.submit_pairs(gids[g], u[o:o + k], v[o:o + k])
+    col.join()
+    wall = time.perf_counter() - t0
+    lat = np.array([x["latency_ms"] for x in done])
+    bad = [x for x in done if x["status"] != 0]
+    if bad:
+        raise RuntimeError(f"{len(bad)} serving requests failed: {bad[:3]}")
+    pairs = sum(x["npairs"] for x in done)
+    edges = sum(m_of[x["graph"]] for x in done if x["kind"] == 0)
+    return {"offered_rate": rate, "wall_s": wall, "requests_per_s": n / wall,
+            "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
+            "intersections_per_s": pairs / wall, "tc_edges_per_s": edges / wall,
+            "max_requests_per_launch": max(x["batch_requests"] for x in done)}
+
+
+def measure_serve(args) -> dict:
+    """Serving workload: saturation throughput from a burst of all requests, then Poisson
+    arrivals at 0.5 / 0.8 / 0.95 of it; an HBM budget below the graphs' full footprint
+    (graphs + a quarter of all counting plans) forces plan eviction and admission waits."""
+    import rtg
+    graphs = serve_setup(SERVE_WORKLOAD["seed"])
+    srv = rtg.Server(0)
+    gids = [srv.add_graph(s, d) for _, s, d in graphs]
+    infos = [srv.graph_info(x) for x in gids]
+    st0 = srv.stats()
+    srv.close()
+    plans = sum((i.m // 256 + i.n + 1) * 8 + (i.n + 1) * 12 + 4096 for i in infos)
+    budget = st0["resident_bytes"] + st0["buffer_bytes"] + plans // 4
+    srv = rtg.Server(0, budget_bytes=budget)
+    gids = [srv.add_graph(s, d) for _, s, d in graphs]
+    rng = np.random.default_rng(SERVE_WORKLOAD["seed"])
+    pools = []
+    for i in infos:
+        pools.append((rng.integers(0, i.n_sym, 250_000, dtype=np.uint32),
+                      rng.integers(0, i.n_sym, 250_000, dtype=np.uint32)))
+    m_of = [int(i.m) for i in infos]
+    nreq = SERVE_WORKLOAD["requests"]
+    # warm-up: every graph's counting plan and both SI slots once
+    warm = serve_requests(np.random.default_rng(1), len(gids), None, 200, pools)
+    serve_run(srv, gids, pools, warm, None, m_of)
+    sat = serve_run(srv, gids, pools, serve_requests(np.random.default_rng(2), len(gids), None,
+                                                     nreq, pools), None, m_of)
+    levels = []
+    for k, f in enumerate(SERVE_WORKLOAD["load_levels"]):
+        reqs = serve_requests(np.random.default_rng(10 + k), len(gids), None, nreq, pools)
+        r = serve_run(srv, gids, pools, reqs, f * sat["requests_per_s"], m_of)
+        r["load"] = f
+        levels.append(r)
+    st = srv.stats()
+    srv.close()
+    return {"saturation": sat, "levels": levels, "budget_bytes": budget,
+            "resident_bytes": st0["resident_bytes"], "plan_bytes_all": plans,
+            "plan_evictions": st["plan_evictions"], "admission_waits": st["admission_waits"],
+            "max_requests_per_launch": st["max_requests_per_launch"],
+            "max_inflight_launches": st["max_inflight_launches"],
+            "tc_coalesced": st["tc_coalesced"], "si_launches": st["si_launches"],
+            "tc_launches": st["tc_launches"]}
+
+
+def run_gpu_serve(args, dist: Dist) -> None:
+    r = measure_serve(args)
+    if dist.rank == 0:
+        mid = next(x for x in r["levels"] if x["load"] == 0.8)
+        line = {"metric": "serving p99 latency", "value": mid["p99_ms"], "unit": "ms",
+                "n_gpus": dist.ws, "steps": SERVE_WORKLOAD["requests"], "warmup": 200,
+                "ms_per_step": 1e3 / mid["requests_per_s"], "higher_is_better": False,
+                "scaling": "weak", "vs_baseline": None, "dtype": "u32",
+                "data": "synthetic (seeded R-MAT graphs and uniform vertex pairs)",
+                "config": dict(SERVE_WORKLOAD, parallelism="single GPU",
+                               value_at="load 0.8 of saturation"),
+                "serving": r}
+        print(json.dumps(line), flush=True)
+
+
 def run_reference(args, dist: Dist) -> None:
     if dist.rank != 0:
         return
@@ -511,7 +648,7 @@ def main() -> None:
     ap.add_argument("--impl", default="rtg", choices=["rtg", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--ref-stride", type=int, default=32)
-    ap.add_argument("--workload", default="tc", choices=["tc", "si"],
+    ap.add_argument("--workload", default="tc", choices=["tc", "si", "serve"],
                     help="tc: R-MAT-21 triangle count (with a batched-SI summary); "
                          "si: the 1e6-pair batched set intersection alone")
     ap.add_argument("--tc-only", action="store_true", help="skip the batched-SI summary")
@@ -521,9 +658,15 @@ def main() -> None:
     dist = Dist("gloo" if args.impl == "reference" else None)
     try:
         if args.impl == "reference":
-            (run_reference_si if args.workload == "si" else run_reference)(args, dist)
+            if args.workload == "serve":
+                if dist.rank == 0:
+                    print(json.dumps({"impl": "reference", "unavailable":
+                                      "the reference has no serving loop: its mains count one "
+                                      "graph or one dataset per process"}), flush=True)
+            else:
+                (run_reference_si if args.workload == "si" else run_reference)(args, dist)
         else:
-            (run_gpu_si if args.workload == "si" else run_gpu)(args, dist)
+            {"tc": run_gpu, "si": run_gpu_si, "serve": run_gpu_serve}[args.workload](args, dist)
     finally:
         dist.close()
 

@@ -64,6 +64,33 @@ class DatasetInfo(C.Structure):
                 ("intersection", C.c_uint32), ("elems", C.c_uint64)]
 
 
+class ServeConfig(C.Structure):
+    _fields_ = [("hbm_budget_bytes", C.c_uint64), ("max_batch_pairs", C.c_uint32),
+                ("si_slots", C.c_uint32), ("max_graphs", C.c_uint32), ("flags", C.c_uint32),
+                ("inject_fail_launch", C.c_uint32), ("reserved", C.c_uint32)]
+
+
+class RequestInfo(C.Structure):
+    _fields_ = [("status", C.c_int), ("kind", C.c_uint32), ("graph", C.c_uint32),
+                ("launches", C.c_uint32), ("batch_requests", C.c_uint32),
+                ("reserved", C.c_uint32), ("npairs", C.c_uint64), ("triangles", C.c_uint64),
+                ("latency_ms", C.c_double), ("queue_ms", C.c_double)]
+
+    def as_dict(self) -> dict:
+        return {k: getattr(self, k) for k, _ in self._fields_ if k != "reserved"}
+
+
+class ServeStats(C.Structure):
+    _fields_ = [(k, C.c_uint64) for k in (
+        "submitted", "completed", "failed", "cancelled", "tc_launches", "tc_coalesced",
+        "si_launches", "si_pairs", "max_requests_per_launch", "max_inflight_launches",
+        "resident_graphs", "resident_bytes", "plan_bytes", "buffer_bytes", "budget_bytes",
+        "plan_evictions", "admission_waits")]
+
+    def as_dict(self) -> dict:
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
 P = C.c_void_p
 u32p = C.POINTER(C.c_uint32)
 u64p = C.POINTER(C.c_uint64)
@@ -114,6 +141,21 @@ _SIGS = {
                                      C.c_uint32, C.POINTER(Timing)]),
     "rtg_si_materialize": (C.c_int, [P, P, P, P, C.c_uint64, P, P, C.c_uint64,
                                      C.POINTER(Timing)]),
+    "rtg_serve_start": (C.c_int, [C.c_int, C.POINTER(ServeConfig), C.POINTER(P)]),
+    "rtg_serve_stop": (None, [P]),
+    "rtg_serve_last_error": (C.c_char_p, [P]),
+    "rtg_serve_add_graph": (C.c_int, [P, P, P, C.c_uint64, u32p]),
+    "rtg_serve_add_graph_file": (C.c_int, [P, C.c_char_p, C.c_int, u32p]),
+    "rtg_serve_remove_graph": (C.c_int, [P, C.c_uint32]),
+    "rtg_serve_graph_info": (C.c_int, [P, C.c_uint32, C.POINTER(GraphInfo)]),
+    "rtg_serve_submit_tc": (C.c_int, [P, C.c_uint32, u64p]),
+    "rtg_serve_submit_pairs": (C.c_int, [P, C.c_uint32, P, P, C.c_uint64, P, u64p]),
+    "rtg_serve_poll": (C.c_int, [P, C.c_uint64, C.c_int32, C.POINTER(RequestInfo)]),
+    "rtg_serve_wait_any": (C.c_int, [P, C.c_int32, u64p, C.POINTER(RequestInfo)]),
+    "rtg_serve_cancel": (C.c_int, [P, C.c_uint64]),
+    "rtg_serve_release": (C.c_int, [P]),
+    "rtg_serve_drain": (C.c_int, [P, C.c_int32]),
+    "rtg_serve_stats_get": (C.c_int, [P, C.POINTER(ServeStats)]),
     "rtg_dataset_read": (C.c_int, [C.c_char_p, C.POINTER(DatasetInfo), P, P]),
     "rtg_dataset_write": (C.c_int, [C.c_char_p, C.POINTER(DatasetInfo), P, P]),
     "rtg_edges_write_bin": (C.c_int, [C.c_char_p, P, P, C.c_uint64]),
@@ -500,3 +542,126 @@ class Sets:
                                               _ptr(off), _ptr(el), capacity, C.byref(t)),
                        "si_materialize")
         return off, el[: int(off[-1])], t
+
+
+# ---------------------------------------------------------------- serving
+
+REQ_TC, REQ_PAIRS = 0, 1
+SERVE_START_HELD = 0x1
+
+
+class Server:
+    """Request loop over resident graphs (rtg_serve_*). Pair arrays and output arrays of
+    submitted requests are kept alive here until their request is collected."""
+
+    def __init__(self, device: int = 0, budget_bytes: int = 0, max_batch_pairs: int = 0,
+                 si_slots: int = 0, max_graphs: int = 0, held: bool = False,
+                 inject_fail_launch: int = 0):
+        cfg = ServeConfig(budget_bytes, max_batch_pairs, si_slots, max_graphs,
+                          SERVE_START_HELD if held else 0, inject_fail_launch, 0)
+        self.h = P()
+        st = lib.rtg_serve_start(device, C.byref(cfg), C.byref(self.h))
+        if st != OK:
+            raise RtgError(st, "serve_start")
+        self._keep: dict[int, tuple] = {}
+
+    def _check(self, st: int, what: str) -> None:
+        if st != OK:
+            raise RtgError(st, f"{what}: {lib.rtg_serve_last_error(self.h).decode()}")
+
+    def close(self) -> None:
+        if self.h:
+            lib.rtg_serve_stop(self.h)
+            self.h = P()
+            self._keep.clear()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def add_graph(self, src: np.ndarray, dst: np.ndarray) -> int:
+        src = np.ascontiguousarray(src, np.uint32)
+        dst = np.ascontiguousarray(dst, np.uint32)
+        gid = C.c_uint32(0)
+        self._check(lib.rtg_serve_add_graph(self.h, _ptr(src), _ptr(dst), len(src),
+                                            C.byref(gid)), "serve_add_graph")
+        return gid.value
+
+    def add_graph_file(self, path: str, fmt: int = FMT_EDGE_BIN) -> int:
+        gid = C.c_uint32(0)
+        self._check(lib.rtg_serve_add_graph_file(self.h, str(path).encode(), fmt, C.byref(gid)),
+                    "serve_add_graph_file")
+        return gid.value
+
+    def remove_graph(self, gid: int) -> None:
+        self._check(lib.rtg_serve_remove_graph(self.h, gid), "serve_remove_graph")
+
+    def graph_info(self, gid: int) -> GraphInfo:
+        info = GraphInfo()
+        self._check(lib.rtg_serve_graph_info(self.h, gid, C.byref(info)), "serve_graph_info")
+        return info
+
+    def submit_tc(self, gid: int) -> int:
+        rid = C.c_uint64(0)
+        self._check(lib.rtg_serve_submit_tc(self.h, gid, C.byref(rid)), "serve_submit_tc")
+        return rid.value
+
+    def submit_pairs(self, gid: int, u: np.ndarray, v: np.ndarray,
+                     out: np.ndarray | None = None) -> tuple[int, np.ndarray]:
+        u = np.ascontiguousarray(u, np.uint32)
+        v = np.ascontiguousarray(v, np.uint32)
+        if len(u) != len(v):
+            raise ValueError("u and v differ in length")
+        if out is None:
+            out = np.empty(max(len(u), 1), np.uint32)
+        rid = C.c_uint64(0)
+        self._check(lib.rtg_serve_submit_pairs(self.h, gid, _ptr(u), _ptr(v), len(u), _ptr(out),
+                                               C.byref(rid)), "serve_submit_pairs")
+        self._keep[rid.value] = (u, v, out)
+        return rid.value, out[: len(u)]
+
+    def poll(self, rid: int, wait_ms: int = -1) -> dict | None:
+        """Info of a completed request, or None while it runs (wait_ms 0 polls)."""
+        info = RequestInfo()
+        st = lib.rtg_serve_poll(self.h, rid, wait_ms, C.byref(info))
+        if st == ERR_BUSY:
+            return None
+        self._check(st, "serve_poll")
+        self._keep.pop(rid, None)
+        return info.as_dict()
+
+    def wait_any(self, wait_ms: int = -1) -> tuple[int, dict] | None:
+        rid = C.c_uint64(0)
+        info = RequestInfo()
+        st = lib.rtg_serve_wait_any(self.h, wait_ms, C.byref(rid), C.byref(info))
+        if st == ERR_BUSY:
+            return None
+        self._check(st, "serve_wait_any")
+        self._keep.pop(rid.value, None)
+        return rid.value, info.as_dict()
+
+    def cancel(self, rid: int) -> None:
+        self._check(lib.rtg_serve_cancel(self.h, rid), "serve_cancel")
+
+    def release(self) -> None:
+        self._check(lib.rtg_serve_release(self.h), "serve_release")
+
+    def drain(self, wait_ms: int = -1) -> bool:
+        st = lib.rtg_serve_drain(self.h, wait_ms)
+        if st == ERR_BUSY:
+            return False
+        self._check(st, "serve_drain")
+        return True
+
+    def stats(self) -> dict:
+        s = ServeStats()
+        self._check(lib.rtg_serve_stats_get(self.h, C.byref(s)), "serve_stats")
+        return s.as_dict()
