@@ -277,6 +277,28 @@ rtg_status rtg_si_materialize(rtg_ctx *ctx, const rtg_sets *s, const uint32_t *p
                               const uint32_t *pair_b, uint64_t npairs, uint64_t *out_offsets,
                               uint32_t *out_elems, uint64_t out_capacity, rtg_timing *timing);
 
+/* --------------------------------------------------------------- autotuning
+ * Time a grid of schedules for the batched forms (after an L2 flush, median of three
+ * runs each), keep the fastest whose result is bit-identical to the default schedule's,
+ * and set it on the context. TC: tc_item_edges x tc_region_words x tc_block_warps. SI:
+ * si_stage_bytes x si_stage_slots x si_block_warps x si_search_ratio, on the pairs given
+ * (host arrays; a representative sample of the workload). With cache_path (a text file,
+ * created if missing) the winner is stored under a key of the device and the workload's
+ * size class, and a later call with the same key applies it without searching. */
+typedef struct rtg_tune_result {
+    rtg_config best;
+    double best_ms;      /* median time of the winner                        */
+    double default_ms;   /* median time of the library default               */
+    uint32_t candidates; /* schedules tried                                   */
+    uint32_t rejected;   /* did not fit the device or did not match the count */
+    uint32_t from_cache; /* 1: taken from the cache, nothing was timed        */
+    uint32_t reserved;
+} rtg_tune_result;
+rtg_status rtg_tune_tc(rtg_ctx *ctx, rtg_graph *g, const char *cache_path, rtg_tune_result *res);
+rtg_status rtg_tune_si(rtg_ctx *ctx, const rtg_sets *s, const uint32_t *pair_a,
+                       const uint32_t *pair_b, uint64_t npairs, const char *cache_path,
+                       rtg_tune_result *res);
+
 /* ----------------------------------------------------------------- serving
  * A request loop over many graphs resident in HBM. No counterpart in the reference,
  * whose mains run one graph or one dataset per process; it serves the reference's two
@@ -338,6 +360,7 @@ typedef struct rtg_serve_stats {
     uint64_t max_inflight_launches;       /* TC + SI launches in flight at one time      */
     uint64_t resident_graphs, resident_bytes, plan_bytes, buffer_bytes, budget_bytes;
     uint64_t plan_evictions, admission_waits;
+    uint64_t tc_direct;  /* TC launches without a cached plan (shared run scratch)       */
 } rtg_serve_stats;
 
 rtg_status rtg_serve_start(int device, const rtg_serve_config *cfg, rtg_server **out);

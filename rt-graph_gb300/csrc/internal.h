@@ -146,8 +146,14 @@ void tc_plan_free(TcPlan *p);
 // stream without waiting; the total lands in the pinned host word *h_total when the
 // stream reaches it. At most one such count of a graph may be in flight.
 rtg_status tc_launch_async(rtg_ctx *ctx, rtg_graph *g, unsigned long long *h_total);
-// Device bytes the batched plan of g will hold (upper estimate).
+// Device bytes the batched plan of g will hold (upper estimate; also the scratch that
+// tc_launch_direct needs).
 uint64_t tc_plan_estimate_bytes(const rtg_ctx *ctx, const rtg_graph *g);
+// The same count without a plan: the kernels are launched directly on ctx's stream with
+// their buffers carved from the caller's device scratch, which must stay untouched until
+// the count has completed.
+rtg_status tc_launch_direct(rtg_ctx *ctx, rtg_graph *g, void *scratch, uint64_t scratch_bytes,
+                            unsigned long long *h_total);
 // Free the batched plan of g (no count of g may be in flight).
 void tc_plan_release(rtg_graph *g);
 

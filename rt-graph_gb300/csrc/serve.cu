@@ -2,7 +2,8 @@
 //
 // One engine thread owns every launch. It keeps
 //   - a build context (graph construction, serialised by build_mu),
-//   - a TC context whose stream replays each graph's captured batched-count graph,
+//   - kTcRuns TC contexts, each with its own stream, that replay a graph's captured
+//     batched-count graph (or launch the count directly into the run's scratch),
 //   - si_slots set-intersection contexts, each with its own stream, pinned staging and
 //     device buffers for one merged launch.
 // Each pass of the engine loop: completes launches whose events have fired (copying
@@ -93,12 +94,15 @@ struct SiSlot {
 };
 
 struct TcRun {
+    rtg_ctx *ctx = nullptr;  // own stream: counts of different graphs overlap
     SGraph *sg = nullptr;
     uint32_t slot = 0;
     std::vector<Req *> reqs;
     unsigned long long *h_total = nullptr;  // pinned
     cudaEvent_t done = nullptr;
     bool busy = false;
+    void *scratch = nullptr;  // direct counts of graphs without a cached plan
+    uint64_t scratch_bytes = 0;
 };
 
 }  // namespace
@@ -277,25 +281,47 @@ void launch_tc(rtg_server *s) {
                 break;
             }
         if (!run) return;
-        if (!g.plan_bytes) {
+        // A graph keeps a captured counting plan when the budget has room for one; otherwise
+        // it is counted with direct launches in the run's own scratch, grown to the largest
+        // graph seen (idle plans are evicted only when that scratch cannot grow otherwise).
+        bool use_plan = g.plan_bytes != 0;
+        if (!use_plan) {
             const uint64_t need = tc_plan_estimate_bytes(s->tcx, g.g);
-            if (!make_room(s, need, &g)) {
-                bool any_running = false;
-                for (TcRun &x : s->runs) any_running |= x.busy;
-                if (!any_running) {  // nothing will free memory: refuse
+            if (used_bytes(s) + need <= s->st.budget_bytes) {
+                g.plan_bytes = need;
+                s->plans += need;
+                use_plan = true;
+            } else if (run->scratch_bytes < need) {
+                const uint64_t grow = need - run->scratch_bytes;
+                if (!make_room(s, grow, &g)) {
+                    bool any_running = false;
+                    for (TcRun &x : s->runs) any_running |= x.busy;
+                    if (!any_running) {  // nothing will free memory: refuse
+                        it = s->tc_queue.erase(it);
+                        r->status = srv_fail(s, RTG_ERR_OOM,
+                                             "count of graph %u needs %llu B beyond the budget",
+                                             r->graph, (unsigned long long)grow);
+                        finish(s, r);
+                        continue;
+                    }
+                    s->st.admission_waits++;
+                    ++it;
+                    continue;
+                }
+                dev_free(run->scratch);  // the run is idle: its last count has completed
+                s->buffers -= run->scratch_bytes;
+                run->scratch = nullptr;
+                run->scratch_bytes = 0;
+                if (dev_alloc(run->ctx, &run->scratch, need) != RTG_OK) {
                     it = s->tc_queue.erase(it);
-                    r->status = srv_fail(s, RTG_ERR_OOM,
-                                         "counting plan of graph %u (%llu B) exceeds the budget",
-                                         r->graph, (unsigned long long)need);
+                    r->status = srv_fail(s, RTG_ERR_OOM, "run scratch of %llu B",
+                                         (unsigned long long)need);
                     finish(s, r);
                     continue;
                 }
-                s->st.admission_waits++;
-                ++it;
-                continue;
+                run->scratch_bytes = need;
+                s->buffers += need;
             }
-            g.plan_bytes = need;
-            s->plans += need;
         }
         // every waiting TC request of this graph shares this launch
         run->reqs.clear();
@@ -311,13 +337,16 @@ void launch_tc(rtg_server *s) {
         const auto now = Clock::now();
         for (Req *q : run->reqs) mark_launched(q, now, (uint32_t)run->reqs.size());
         s->st.tc_coalesced += run->reqs.size() - 1;
-        rtg_status st = tc_launch_async(s->tcx, g.g, run->h_total);
+        rtg_status st = use_plan ? tc_launch_async(run->ctx, g.g, run->h_total)
+                                 : tc_launch_direct(run->ctx, g.g, run->scratch,
+                                                    run->scratch_bytes, run->h_total);
+        if (!use_plan) s->st.tc_direct++;
         if (st == RTG_OK) {
-            cudaError_t e = cudaEventRecord(run->done, s->tcx->stream);
-            if (e != cudaSuccess) st = cuda_fail(s->tcx, e, "event", __FILE__, __LINE__);
+            cudaError_t e = cudaEventRecord(run->done, run->ctx->stream);
+            if (e != cudaSuccess) st = cuda_fail(run->ctx, e, "event", __FILE__, __LINE__);
         }
         if (st != RTG_OK) {
-            srv_fail(s, st, "triangle count of graph %u: %s", r->graph, rtg_last_error(s->tcx));
+            srv_fail(s, st, "triangle count of graph %u: %s", r->graph, rtg_last_error(run->ctx));
             for (Req *q : run->reqs) {
                 q->status = st;
                 finish(s, q);
@@ -485,7 +514,7 @@ rtg_status add_built_graph(rtg_server *s, rtg_graph *g, uint32_t *graph_id) {
     std::lock_guard<std::mutex> lk(s->mu);
     rtg_status st = RTG_OK;
     if (s->stopping) st = srv_fail(s, RTG_ERR_STATE, "server is stopping");
-    else if (used_bytes(s) + bytes > s->st.budget_bytes)
+    else if (used_bytes(s) + bytes > s->st.budget_bytes && !make_room(s, bytes, nullptr))
         st = srv_fail(s, RTG_ERR_OOM, "graph needs %llu B; %llu of %llu B in use",
                       (unsigned long long)bytes, (unsigned long long)used_bytes(s),
                       (unsigned long long)s->st.budget_bytes);
@@ -595,6 +624,7 @@ rtg_status rtg_serve_start(int device, const rtg_serve_config *cfg, rtg_server *
     for (uint32_t i = 0; i < kTcRuns; ++i) {
         TcRun &r = s->runs[i];
         r.slot = i;
+        if ((st = rtg_init(device, &r.ctx)) != RTG_OK) return bail(st);
         if (cudaMallocHost((void **)&r.h_total, 64) != cudaSuccess) return bail(RTG_ERR_OOM);
         if (cudaEventCreateWithFlags(&r.done, cudaEventDisableTiming) != cudaSuccess)
             return bail(RTG_ERR_DEVICE);
@@ -646,8 +676,11 @@ void rtg_serve_stop(rtg_server *s) {
         rtg_destroy(sl.ctx);
     }
     for (TcRun &r : s->runs) {
+        if (r.ctx) cudaStreamSynchronize(r.ctx->stream);
+        dev_free(r.scratch);
         if (r.h_total) cudaFreeHost(r.h_total);
         if (r.done) cudaEventDestroy(r.done);
+        rtg_destroy(r.ctx);
     }
     if (s->h_tab) cudaFreeHost(s->h_tab);
     rtg_destroy(s->tcx);

@@ -376,6 +376,67 @@ bool same_tc_config(const rtg_config &a, const rtg_config &b) {
            a.tc_block_warps == b.tc_block_warps && a.tc_blocks_per_sm == b.tc_blocks_per_sm;
 }
 
+// Launch shape of the batched count of one graph under one schedule.
+struct BatchedShape {
+    WarpCfg pc;
+    uint32_t W;
+    size_t smem;
+    int grid, g1;
+    uint64_t item_cap;
+    size_t cub_bytes;
+};
+
+rtg_status batched_shape(rtg_ctx *ctx, const CountCsr &c, const rtg_config &cfg,
+                         BatchedShape *bs) {
+    bs->W = cfg.tc_block_warps;
+    bs->pc.E = cfg.tc_item_edges;
+    bs->pc.R = cfg.tc_region_words;
+    bs->pc.n = c.n;
+    bs->smem = (size_t)bs->W * bs->pc.R * 4;
+    if (bs->smem + 256 > (size_t)ctx->smem_optin)
+        return fail(ctx, RTG_ERR_INVALID_ARG, "schedule needs %zu B of shared memory", bs->smem);
+    bs->item_cap = c.m / bs->pc.E + c.n + 1;
+    bs->cub_bytes = 0;
+    RTG_CUDA(ctx, cub::DeviceScan::ExclusiveSum(nullptr, bs->cub_bytes, (uint32_t *)nullptr,
+                                                (uint32_t *)nullptr, (int64_t)c.n + 1,
+                                                ctx->stream));
+    RTG_CUDA(ctx, cudaFuncSetAttribute(k_tc_warp, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)bs->smem));
+    int per_sm = 0;
+    RTG_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_tc_warp, bs->W * 32,
+                                                                bs->smem));
+    if (cfg.tc_blocks_per_sm) per_sm = std::min<int>(per_sm, (int)cfg.tc_blocks_per_sm);
+    per_sm = std::max(per_sm, 1);
+    bs->grid = ctx->sm_count * per_sm;
+    bs->g1 = (int)std::max<uint64_t>(1, std::min<uint64_t>((c.n + 256ull) / 256,
+                                                          ctx->sm_count * 16ull));
+    return RTG_OK;
+}
+
+// reset -> item counts -> scan -> item fill -> [k0] persistent count [k1]
+void enqueue_batched(cudaStream_t st, const CountCsr &c, const BatchedShape &bs, uint64_t *items,
+                     uint32_t *vcnt, void *cub_tmp, unsigned long long *acc, cudaEvent_t k0,
+                     cudaEvent_t k1, bool external_events) {
+    uint32_t *vbase = vcnt + (c.n + 1ull);
+    size_t cub_bytes = bs.cub_bytes;
+    cudaMemsetAsync(acc, 0, 8 * sizeof(unsigned long long), st);
+    k_item_counts<<<bs.g1, 256, 0, st>>>(c.off, c.in_off, c.n, bs.pc.E, vcnt);
+    cub::DeviceScan::ExclusiveSum(cub_tmp, cub_bytes, vcnt, vbase, (int64_t)c.n + 1, st);
+    k_item_fill<<<bs.g1, 256, 0, st>>>(c.off, c.in_off, c.n, bs.pc.E, vbase, items, acc);
+    if (k0) {
+        if (external_events) cudaEventRecordWithFlags(k0, st, cudaEventRecordExternal);
+        else cudaEventRecord(k0, st);
+    }
+    k_tc_warp<<<bs.grid, bs.W * 32, bs.smem, st>>>(c.off, c.adj, c.in_off, c.in_rng, items, acc,
+                                                   bs.pc);
+    if (k1) {
+        if (external_events) cudaEventRecordWithFlags(k1, st, cudaEventRecordExternal);
+        else cudaEventRecord(k1, st);
+    }
+}
+
+constexpr uint64_t kBatchedKernels = 5;  // item counts, scan (init + sweep), item fill, count
+
 rtg_status batched_plan(rtg_ctx *ctx, rtg_graph *g, TcPlan **out) {
     rtg_config cfg = effective_config(ctx);
     if (g->plan_batched && same_tc_config(g->plan_batched->cfg, cfg)) {
@@ -394,56 +455,22 @@ rtg_status batched_plan(rtg_ctx *ctx, rtg_graph *g, TcPlan **out) {
     const CountCsr &c = g->cnt;
     if (!c.built)
         return bail(fail(ctx, RTG_ERR_STATE, "counting form of the CSR is missing"));
-    const uint32_t E = cfg.tc_item_edges, W = cfg.tc_block_warps;
-    WarpCfg pc{};
-    pc.E = E;
-    pc.R = cfg.tc_region_words;
-    pc.n = c.n;
-    const size_t smem = (size_t)W * pc.R * 4;
-    if (smem + 256 > (size_t)ctx->smem_optin)
-        return bail(fail(ctx, RTG_ERR_INVALID_ARG, "schedule needs %zu B of shared memory", smem));
-
-    const uint64_t item_cap = c.m / E + c.n + 1;
+    BatchedShape bs{};
     rtg_status s;
-    if ((s = dev_alloc(ctx, (void **)&p->items, item_cap * 8)) != RTG_OK) return bail(s);
+    if ((s = batched_shape(ctx, c, cfg, &bs)) != RTG_OK) return bail(s);
+    if ((s = dev_alloc(ctx, (void **)&p->items, bs.item_cap * 8)) != RTG_OK) return bail(s);
     if ((s = dev_alloc(ctx, (void **)&p->vcnt, (c.n + 1ull) * 4 * 2)) != RTG_OK) return bail(s);
     if ((s = dev_alloc(ctx, (void **)&p->acc, 8 * sizeof(unsigned long long))) != RTG_OK)
         return bail(s);
-    uint32_t *vbase = p->vcnt + (c.n + 1ull);
-    size_t cub_bytes = 0;
-    cudaError_t e = cub::DeviceScan::ExclusiveSum(nullptr, cub_bytes, p->vcnt, vbase,
-                                                  (int64_t)c.n + 1, ctx->stream);
-    if (e != cudaSuccess) return bail(cuda_fail(ctx, e, "scan size", __FILE__, __LINE__));
-    if ((s = dev_alloc(ctx, &p->cub_tmp, cub_bytes)) != RTG_OK) return bail(s);
+    if ((s = dev_alloc(ctx, &p->cub_tmp, bs.cub_bytes)) != RTG_OK) return bail(s);
+    cudaError_t e;
     if ((e = cudaEventCreate(&p->k0)) != cudaSuccess ||
         (e = cudaEventCreate(&p->k1)) != cudaSuccess)
         return bail(cuda_fail(ctx, e, "event", __FILE__, __LINE__));
-    if ((e = cudaFuncSetAttribute(k_tc_warp, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                  (int)smem)) != cudaSuccess)
-        return bail(cuda_fail(ctx, e, "smem attribute", __FILE__, __LINE__));
-    int per_sm = 0;
-    if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_tc_warp, W * 32, smem)) !=
-        cudaSuccess)
-        return bail(cuda_fail(ctx, e, "occupancy", __FILE__, __LINE__));
-    if (cfg.tc_blocks_per_sm) per_sm = std::min<int>(per_sm, (int)cfg.tc_blocks_per_sm);
-    per_sm = std::max(per_sm, 1);
-    const int grid = ctx->sm_count * per_sm;
-    const int g1 = (int)std::max<uint64_t>(1, std::min<uint64_t>((c.n + 256ull) / 256,
-                                                                  ctx->sm_count * 16ull));
-
-    // capture: reset -> item counts -> scan -> item fill -> [ev] persistent count [ev]
     if ((e = cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal)) !=
         cudaSuccess)
         return bail(cuda_fail(ctx, e, "capture", __FILE__, __LINE__));
-    cudaMemsetAsync(p->acc, 0, 8 * sizeof(unsigned long long), ctx->stream);
-    k_item_counts<<<g1, 256, 0, ctx->stream>>>(c.off, c.in_off, c.n, E, p->vcnt);
-    cub::DeviceScan::ExclusiveSum(p->cub_tmp, cub_bytes, p->vcnt, vbase, (int64_t)c.n + 1,
-                                  ctx->stream);
-    k_item_fill<<<g1, 256, 0, ctx->stream>>>(c.off, c.in_off, c.n, E, vbase, p->items, p->acc);
-    cudaEventRecordWithFlags(p->k0, ctx->stream, cudaEventRecordExternal);
-    k_tc_warp<<<grid, W * 32, smem, ctx->stream>>>(c.off, c.adj, c.in_off, c.in_rng, p->items,
-                                                   p->acc, pc);
-    cudaEventRecordWithFlags(p->k1, ctx->stream, cudaEventRecordExternal);
+    enqueue_batched(ctx->stream, c, bs, p->items, p->vcnt, p->cub_tmp, p->acc, p->k0, p->k1, true);
     e = cudaStreamEndCapture(ctx->stream, &p->graph);
     if (e != cudaSuccess) return bail(cuda_fail(ctx, e, "end capture", __FILE__, __LINE__));
     if ((e = cudaGraphInstantiate(&p->exec, p->graph, 0)) != cudaSuccess)
@@ -577,6 +604,36 @@ uint64_t tc_plan_estimate_bytes(const rtg_ctx *ctx, const rtg_graph *g) {
     const CountCsr &c = g->cnt;
     // items + vertex counts + scan temporary (bounded by one word per vertex) + totals
     return (c.m / cfg.tc_item_edges + c.n + 1) * 8 + (c.n + 1ull) * 8 + (c.n + 1ull) * 4 + 4096;
+}
+
+rtg_status tc_launch_direct(rtg_ctx *ctx, rtg_graph *g, void *scratch, uint64_t scratch_bytes,
+                            unsigned long long *h_total) {
+    const CountCsr &c = g->cnt;
+    if (!c.built) return fail(ctx, RTG_ERR_STATE, "counting form of the CSR is missing");
+    if (c.n > 0x7FFFFFFFu || c.m >= (1ull << 32))
+        return fail(ctx, RTG_ERR_INVALID_ARG, "graph too large for 32-bit edge ids");
+    if (c.m == 0) {
+        *h_total = 0;
+        return RTG_OK;
+    }
+    if (tc_plan_estimate_bytes(ctx, g) > scratch_bytes)
+        return fail(ctx, RTG_ERR_INVALID_ARG, "scratch too small for the count");
+    BatchedShape bs{};
+    RTG_TRY(batched_shape(ctx, c, effective_config(ctx), &bs));
+    // scratch: acc (64 B) | items | vertex counts and offsets | scan temporary
+    char *p = static_cast<char *>(scratch);
+    unsigned long long *acc = reinterpret_cast<unsigned long long *>(p);
+    uint64_t *items = reinterpret_cast<uint64_t *>(p + 64);
+    uint32_t *vcnt = reinterpret_cast<uint32_t *>(items + bs.item_cap);
+    void *tmp = reinterpret_cast<void *>(
+        (reinterpret_cast<uintptr_t>(vcnt + 2 * (c.n + 1ull)) + 255) & ~(uintptr_t)255);
+    if ((uint64_t)(static_cast<char *>(tmp) - p) + bs.cub_bytes > scratch_bytes)
+        return fail(ctx, RTG_ERR_INVALID_ARG, "scratch too small for the count");
+    enqueue_batched(ctx->stream, c, bs, items, vcnt, tmp, acc, nullptr, nullptr, false);
+    RTG_CUDA(ctx, cudaGetLastError());
+    ctx->launches += kBatchedKernels;
+    RTG_CUDA(ctx, cudaMemcpyAsync(h_total, acc, 8, cudaMemcpyDeviceToHost, ctx->stream));
+    return RTG_OK;
 }
 
 rtg_status tc_launch_async(rtg_ctx *ctx, rtg_graph *g, unsigned long long *h_total) {

@@ -64,6 +64,17 @@ class DatasetInfo(C.Structure):
                 ("intersection", C.c_uint32), ("elems", C.c_uint64)]
 
 
+class TuneResult(C.Structure):
+    _fields_ = [("best", Config), ("best_ms", C.c_double), ("default_ms", C.c_double),
+                ("candidates", C.c_uint32), ("rejected", C.c_uint32),
+                ("from_cache", C.c_uint32), ("reserved", C.c_uint32)]
+
+    def as_dict(self) -> dict:
+        return {"best": self.best.as_dict(), "best_ms": self.best_ms,
+                "default_ms": self.default_ms, "candidates": self.candidates,
+                "rejected": self.rejected, "from_cache": bool(self.from_cache)}
+
+
 class ServeConfig(C.Structure):
     _fields_ = [("hbm_budget_bytes", C.c_uint64), ("max_batch_pairs", C.c_uint32),
                 ("si_slots", C.c_uint32), ("max_graphs", C.c_uint32), ("flags", C.c_uint32),
@@ -85,7 +96,7 @@ class ServeStats(C.Structure):
         "submitted", "completed", "failed", "cancelled", "tc_launches", "tc_coalesced",
         "si_launches", "si_pairs", "max_requests_per_launch", "max_inflight_launches",
         "resident_graphs", "resident_bytes", "plan_bytes", "buffer_bytes", "budget_bytes",
-        "plan_evictions", "admission_waits")]
+        "plan_evictions", "admission_waits", "tc_direct")]
 
     def as_dict(self) -> dict:
         return {k: getattr(self, k) for k, _ in self._fields_}
@@ -141,6 +152,8 @@ _SIGS = {
                                      C.c_uint32, C.POINTER(Timing)]),
     "rtg_si_materialize": (C.c_int, [P, P, P, P, C.c_uint64, P, P, C.c_uint64,
                                      C.POINTER(Timing)]),
+    "rtg_tune_tc": (C.c_int, [P, P, C.c_char_p, C.POINTER(TuneResult)]),
+    "rtg_tune_si": (C.c_int, [P, P, P, P, C.c_uint64, C.c_char_p, C.POINTER(TuneResult)]),
     "rtg_serve_start": (C.c_int, [C.c_int, C.POINTER(ServeConfig), C.POINTER(P)]),
     "rtg_serve_stop": (None, [P]),
     "rtg_serve_last_error": (C.c_char_p, [P]),
@@ -450,6 +463,13 @@ class Graph:
         self.ctx.check(lib.rtg_graph_info_get(self.h, C.byref(i)))
         return i
 
+    def tune(self, cache: str | None = None) -> dict:
+        """Autotune the batched count's schedule for this graph (set on the context)."""
+        r = TuneResult()
+        self.ctx.check(lib.rtg_tune_tc(self.ctx.h, self.h, cache.encode() if cache else None,
+                                       C.byref(r)), "tune_tc")
+        return r.as_dict()
+
     def csr(self, symmetric: bool = False):
         i = self.info()
         n, m = (i.n_sym, i.m_sym) if symmetric else (i.n, i.m)
@@ -524,6 +544,16 @@ class Sets:
         self.ctx.check(lib.rtg_si_count_dense(self.ctx.h, self.h, a0, a1, b0, b1, _ptr(out),
                                               family, C.byref(t)), "si_count_dense")
         return out[: (a1 - a0) * (b1 - b0)], t
+
+    def tune(self, pa: np.ndarray, pb: np.ndarray, cache: str | None = None) -> dict:
+        """Autotune the batched SI schedule on these pairs (set on the context)."""
+        pa = np.ascontiguousarray(pa, np.uint32)
+        pb = np.ascontiguousarray(pb, np.uint32)
+        r = TuneResult()
+        self.ctx.check(lib.rtg_tune_si(self.ctx.h, self.h, _ptr(pa), _ptr(pb), len(pa),
+                                       cache.encode() if cache else None, C.byref(r)),
+                       "tune_si")
+        return r.as_dict()
 
     def materialize(self, pa: np.ndarray, pb: np.ndarray, capacity: int | None = None):
         pa = np.ascontiguousarray(pa, np.uint32)

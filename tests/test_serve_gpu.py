@@ -172,6 +172,7 @@ def test_budget_admission_and_plan_eviction(graphs):
                 assert info["triangles"] == graphs[k]["tri"]
         st = srv.stats()
     assert st["plan_evictions"] > 0
+    assert st["tc_direct"] > 0  # counted in run scratch when no plan fit
     assert st["resident_graphs"] == 3
 
 
