@@ -278,6 +278,7 @@ def measure_si(args, dist: Dist, ctx, cpu: bool) -> dict:
     off, el, pa, pb, exp = gen_si_workload()
     sets = ctx.sets(off, el)
     np_ = len(pa)
+    tune = sets.tune(pa, pb)  # autotuned schedule of the batched kernel (set on the context)
     algo = si_algo_bytes(off, pa, pb)
     for _ in range(args.warmup):
         ctx.flush_l2()
@@ -341,6 +342,7 @@ def measure_si(args, dist: Dist, ctx, cpu: bool) -> dict:
                      "algo_bytes_per_launch": algo},
         "clocks": clk.summary(),
         "cpu_baseline": None,
+        "schedule": tune,
     }
     if cpu and dist.rank == 0 and dist.ws == 1:
         res["cpu_baseline"] = cpu_baseline_si(off, el, pa, pb)
@@ -360,7 +362,8 @@ def run_gpu_si(args, dist: Dist) -> None:
                 "config": dict(r["config"], parallelism="replicas" if dist.ws > 1 else "single GPU"),
                 "e2e": r["e2e"], "plain": r["plain"], "batched_over_plain": r["batched_over_plain"],
                 "roofline": r["roofline"], "cpu_baseline": r["cpu_baseline"],
-                "clocks": r["clocks"], "gpu_launches": r["launches"]}
+                "clocks": r["clocks"], "gpu_launches": r["launches"],
+                "schedule": r["schedule"]}
         print(json.dumps(line), flush=True)
     ctx.close()
 
@@ -546,6 +549,7 @@ def run_gpu(args, dist: Dist) -> None:
     g.release_edges()
     info = g.info()
     m = info.m
+    tune = g.tune()  # autotuned schedule of the batched count (set on the context)
     # warm-up (also builds and captures the CUDA graph of the batched count)
     for _ in range(args.warmup):
         ctx.flush_l2()
@@ -635,7 +639,7 @@ def run_gpu(args, dist: Dist) -> None:
                           "ms_per_step": sum(plain_ms) / len(plain_ms)},
                 "batched_over_plain": value / plain_value,
                 "roofline": roofline, "cpu_baseline": cpu, "clocks": clk.summary(),
-                "gpu_launches": int(launches), "si": si}
+                "gpu_launches": int(launches), "schedule": tune, "si": si}
         print(json.dumps(line), flush=True)
     ctx.close()
 

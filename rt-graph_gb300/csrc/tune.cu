@@ -125,7 +125,9 @@ extern "C" rtg_status rtg_tune_tc(rtg_ctx *ctx, rtg_graph *g, const char *cache_
         *ms = median(v);
         return RTG_OK;
     };
-    rtg_config def{};
+    // the SI fields of the context's schedule are kept as they are
+    rtg_config def = saved;
+    def.tc_item_edges = def.tc_region_words = def.tc_block_warps = def.tc_blocks_per_sm = 0;
     uint64_t want = 0;
     double def_ms = 0;
     rtg_status st = run(def, &want, &def_ms);
@@ -138,7 +140,7 @@ extern "C" rtg_status rtg_tune_tc(rtg_ctx *ctx, rtg_graph *g, const char *cache_
     for (uint32_t E : {128u, 256u, 512u})
         for (uint32_t R : {512u, 1024u, 2048u})
             for (uint32_t W : {4u, 8u, 16u}) {
-                rtg_config c{};
+                rtg_config c = def;
                 c.tc_item_edges = E;
                 c.tc_region_words = R;
                 c.tc_block_warps = W;
@@ -227,7 +229,10 @@ extern "C" rtg_status rtg_tune_si(rtg_ctx *ctx, const rtg_sets *s, const uint32_
         *ms = median(v);
         return RTG_OK;
     };
-    rtg_config def{};
+    // the TC fields of the context's schedule are kept as they are
+    rtg_config def = saved;
+    def.si_block_warps = def.si_search_ratio = def.si_stage_slots = def.si_stage_bytes = 0;
+    def.si_blocks_per_sm = 0;
     double def_ms = 0;
     rtg_status st = run(def, dwant, &def_ms);
     if (st != RTG_OK) {
@@ -241,7 +246,7 @@ extern "C" rtg_status rtg_tune_si(rtg_ctx *ctx, const rtg_sets *s, const uint32_
         for (uint32_t S : {2u, 3u, 4u})
             for (uint32_t W : {4u, 8u, 16u})
                 for (uint32_t ratio : {16u, 32u, 64u}) {
-                    rtg_config c{};
+                    rtg_config c = def;
                     c.si_stage_bytes = B;
                     c.si_stage_slots = S;
                     c.si_block_warps = W;
