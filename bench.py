@@ -300,6 +300,10 @@ def measure_si(args, dist: Dist, ctx, cpu: bool) -> dict:
     dist.barrier()
     launches = ctx.launches - l0  # kernels only: the L2 flush is a memset
     value, ms = aggregate(dist, np_, sum(ms_steps) / len(ms_steps))
+    # the PLAIN form runs with the library's fixed default schedule, not the tuned one
+    tuned = ctx.config().as_dict()
+    ctx.set_config(**dict(tuned, si_block_warps=0, si_search_ratio=0, si_stage_slots=0,
+                          si_stage_bytes=0, si_blocks_per_sm=0))
     plain_ms = []
     for _ in range(args.steps):
         ctx.flush_l2()
@@ -307,6 +311,7 @@ def measure_si(args, dist: Dist, ctx, cpu: bool) -> dict:
         plain_ms.append(t.count_ms)
         if not np.array_equal(got, exp):
             raise RuntimeError("plain SI counts differ from the expected counts")
+    ctx.set_config(**tuned)
     plain_value, _ = aggregate(dist, np_, sum(plain_ms) / len(plain_ms))
     hpa = ctx.host_array(np_, np.uint32)
     hpb = ctx.host_array(np_, np.uint32)
@@ -620,7 +625,7 @@ def run_gpu(args, dist: Dist) -> None:
                                                "d2h_bytes_per_step")},
               "roofline": {k: r["roofline"][k] for k in ("achieved", "peak", "unit", "frac",
                                                          "traffic", "kernel")},
-              "gpu_launches": r["launches"]}
+              "gpu_launches": r["launches"], "schedule": r["schedule"]["best"]}
     if dist.rank == 0:
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": dist.ws,
                 "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
