@@ -188,8 +188,10 @@ enum : uint32_t { kJobPacked = 0, kJobChunk = 1, kJobChunkLast = 2 };
 enum : uint32_t { kPairZero = 0, kPairPacked = 1, kPairChunked = 2, kPairSkewed = 3 };
 
 // Count the common elements met on diagonals [x0, x1) of the merge of two sorted unique
-// lists in shared memory (ties take A first): a B element is common when it equals the A
-// element consumed just before it. The step is branch-free, one shared load per step.
+// lists in shared memory, each followed by a kEmpty sentinel (elements are below kEmpty, so
+// an exhausted list never wins a comparison). Ties take A first; a common element is
+// counted at the step that consumes its A copy, where both heads are equal. The step is
+// branch-free with one shared load.
 __device__ __forceinline__ uint32_t merge_range_count(const uint32_t *A, uint32_t na,
                                                       const uint32_t *B, uint32_t nb,
                                                       uint32_t x0, uint32_t x1) {
@@ -199,20 +201,14 @@ __device__ __forceinline__ uint32_t merge_range_count(const uint32_t *A, uint32_
         if (A[mid] <= B[x0 - 1 - mid]) lo = mid + 1;
         else hi = mid;
     }
-    uint32_t i = lo, j = x0 - lo;
-    // i == 0: every B element consumed before A[0] is smaller than A[0], so the sentinel
-    // never equals one of them
-    uint32_t last = i ? A[i - 1] : kEmpty;
-    uint32_t ai = A[min(i, na - 1)], bj = B[min(j, nb - 1)];
-    uint32_t c = 0;
+    const uint32_t *pa = A + lo, *pb = B + (x0 - lo);
+    uint32_t ai = *pa, bj = *pb, c = 0;
     for (uint32_t d = x0; d < x1; ++d) {
-        const bool ta = i < na && (j >= nb || ai <= bj);
-        c += (!ta && bj == last) ? 1u : 0u;
-        last = ta ? ai : last;
-        i += ta ? 1u : 0u;
-        j += ta ? 0u : 1u;
-        const uint32_t *src = ta ? A + min(i, na - 1) : B + min(j, nb - 1);
-        const uint32_t v = *src;
+        const bool ta = ai <= bj;
+        c += (ai == bj) ? 1u : 0u;
+        pa += ta ? 1 : 0;
+        pb += ta ? 0 : 1;
+        const uint32_t v = *(ta ? pa : pb);
         ai = ta ? v : ai;
         bj = ta ? bj : v;
     }
@@ -258,9 +254,10 @@ __global__ void k_si_stream(SiArgs s, uint32_t *out, unsigned long long *head, S
         bt.w = 0;
         uint32_t len = 0;
         if (bt.r.valid && bt.r.a > 0) {
+            // words reserved in a slot: each widened list plus one word for its sentinel
             const uint32_t hA = (uint32_t)(reinterpret_cast<uintptr_t>(bt.r.A) & 15u) >> 2;
             const uint32_t hB = (uint32_t)(reinterpret_cast<uintptr_t>(bt.r.B) & 15u) >> 2;
-            const uint64_t ww = (((uint64_t)hA + bt.r.a + 3) & ~3ull) + (((uint64_t)hB + bt.r.b + 3) & ~3ull);
+            const uint64_t ww = (((uint64_t)hA + bt.r.a + 4) & ~3ull) + (((uint64_t)hB + bt.r.b + 4) & ~3ull);
             if (ww <= p.slot_words) {
                 bt.kind = kPairPacked;
                 bt.w = (uint32_t)ww;
@@ -320,24 +317,26 @@ __global__ void k_si_stream(SiArgs s, uint32_t *out, unsigned long long *head, S
                 const unsigned bm = __ballot_sync(kFull, brk);
                 const uint32_t e1 = bm ? (uint32_t)(__ffs(bm) - 1) : 32u;
                 const uint32_t nseg = e1 - e;
-                const uint32_t totW = __shfl_sync(kFull, cur.sw, e1 - 1) - baseW;
                 const uint32_t L = __shfl_sync(kFull, cur.sl, e1 - 1) - baseL;
                 const bool mine = me >= e && me < e1;
-                uint32_t dst = 0, hA = 0, hB = 0, wa = 0;
+                const bool copies = mine && cur.kind == kPairPacked;
+                uint32_t dst = 0, hA = 0, hB = 0, wa = 0, ca = 0, cb = 0;
                 if (mine) {
                     const uint32_t sg = me - e;
                     dst = cur.sw - cur.w - baseW;
-                    const bool pk_ = cur.kind == kPairPacked;
                     hA = (uint32_t)(reinterpret_cast<uintptr_t>(cur.r.A) & 15u) >> 2;
                     hB = (uint32_t)(reinterpret_cast<uintptr_t>(cur.r.B) & 15u) >> 2;
-                    wa = (hA + cur.r.a + 3) & ~3u;
-                    mt[kP + sg] = cur.sl - (pk_ ? cur.r.a + cur.r.b : 0u) - baseL;
+                    wa = (hA + cur.r.a + 4) & ~3u;  // A's words + sentinel, 16-byte multiple
+                    ca = copies ? (hA + cur.r.a + 3) & ~3u : 0u;  // words copied
+                    cb = copies ? (hB + cur.r.b + 3) & ~3u : 0u;
+                    mt[kP + sg] = cur.sl - (copies ? cur.r.a + cur.r.b : 0u) - baseL;
                     mt[kOffA + sg] = dst + hA;
-                    mt[kLenA + sg] = pk_ ? cur.r.a : 0u;
+                    mt[kLenA + sg] = copies ? cur.r.a : 0u;
                     mt[kOffB + sg] = dst + wa + hB;
-                    mt[kLenB + sg] = pk_ ? cur.r.b : 0u;
+                    mt[kLenB + sg] = copies ? cur.r.b : 0u;
                     mt[kOut + sg] = me;
                 }
+                const uint32_t tx = __reduce_add_sync(kFull, (ca + cb) * 4u);
                 if (lane == 0) {
                     mt[0] = nseg;
                     mt[1] = kJobPacked;
@@ -345,15 +344,15 @@ __global__ void k_si_stream(SiArgs s, uint32_t *out, unsigned long long *head, S
                     mt[3] = (uint32_t)(cur.base >> 32);
                     mt[4] = L;
                     mt[kP + nseg] = L;
-                    mbar_arrive_expect_tx(bar, totW * 4u);
+                    mbar_arrive_expect_tx(bar, tx);
                 }
                 __syncwarp();
-                if (mine && cur.kind == kPairPacked) {
+                if (copies) {
                     const uintptr_t gaa = reinterpret_cast<uintptr_t>(cur.r.A) & ~(uintptr_t)15;
                     const uintptr_t gbb = reinterpret_cast<uintptr_t>(cur.r.B) & ~(uintptr_t)15;
-                    bulk_copy_g2s(slot + dst, reinterpret_cast<const void *>(gaa), wa * 4u, bar);
-                    bulk_copy_g2s(slot + dst + wa, reinterpret_cast<const void *>(gbb),
-                                  (cur.w - wa) * 4u, bar);
+                    bulk_copy_g2s(slot + dst, reinterpret_cast<const void *>(gaa), ca * 4u, bar);
+                    bulk_copy_g2s(slot + dst + wa, reinterpret_cast<const void *>(gbb), cb * 4u,
+                                  bar);
                 }
                 e = e1;
                 return true;
@@ -405,6 +404,7 @@ __global__ void k_si_stream(SiArgs s, uint32_t *out, unsigned long long *head, S
             const uintptr_t gaa = ga & ~(uintptr_t)15, gbb = gb & ~(uintptr_t)15;
             const uint32_t hA = (uint32_t)(ga - gaa) >> 2, hB = (uint32_t)(gb - gbb) >> 2;
             const uint32_t bytesA = ((hA + na) * 4u + 15u) & ~15u;
+            const uint32_t resA = ((hA + na + 1) * 4u + 15u) & ~15u;  // + sentinel word
             const uint32_t bytesB = ((hB + nbb) * 4u + 15u) & ~15u;
             mt[0] = 1;
             mt[1] = last ? kJobChunkLast : kJobChunk;
@@ -415,12 +415,12 @@ __global__ void k_si_stream(SiArgs s, uint32_t *out, unsigned long long *head, S
             mt[kP + 1] = na + nbb;
             mt[kOffA] = hA;
             mt[kLenA] = na;
-            mt[kOffB] = bytesA / 4 + hB;
+            mt[kOffB] = resA / 4 + hB;
             mt[kLenB] = nbb;
             mt[kOut] = 0;
             mbar_arrive_expect_tx(bar, bytesA + bytesB);
             bulk_copy_g2s(slot, reinterpret_cast<const void *>(gaa), bytesA, bar);
-            bulk_copy_g2s(slot + bytesA / 4, reinterpret_cast<const void *>(gbb), bytesB, bar);
+            bulk_copy_g2s(slot + resA / 4, reinterpret_cast<const void *>(gbb), bytesB, bar);
         }
         return true;
     };
@@ -448,8 +448,14 @@ __global__ void k_si_stream(SiArgs s, uint32_t *out, unsigned long long *head, S
         }
         phase ^= 1u << sr;
         const uint32_t *mt = meta + sr * kMetaWords;
-        const uint32_t *slot = ring + (size_t)sr * p.slot_words;
+        uint32_t *slot = ring + (size_t)sr * p.slot_words;
         const uint32_t nseg = mt[0], kind = mt[1], L = mt[4];
+        // a sentinel after every list of the slot (its reserved word; copies have landed)
+        if ((uint32_t)lane < nseg && mt[kLenA + lane]) {
+            slot[mt[kOffA + lane] + mt[kLenA + lane]] = kEmpty;
+            slot[mt[kOffB + lane] + mt[kLenB + lane]] = kEmpty;
+        }
+        __syncwarp();
         uint32_t d0 = (uint32_t)(((uint64_t)L * (uint32_t)lane) >> 5);
         const uint32_t d1 = (uint32_t)(((uint64_t)L * (uint32_t)(lane + 1)) >> 5);
         if (d0 < d1) {

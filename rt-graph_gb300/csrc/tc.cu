@@ -190,15 +190,16 @@ struct WarpCfg {
 // as a sequence of 32-element blocks, one coalesced 32-bit load per lane per block; a block
 // never spans two suffixes. kDepth blocks are in flight ahead of the block being tested, and
 // the pipeline runs across edge and batch boundaries; the ranges of the next 32 in-edges
-// are loaded one batch ahead. f(w) tests one element (valid elements only).
+// are loaded one batch ahead. Lanes past the end of a suffix get `idle`; with kSkipIdle
+// they are not tested, otherwise f(idle) must be 0. f(w) tests one element. The per-lane
+// count of one item fits 32 bits (at most E in-edges of at most n elements each / 32).
 constexpr int kDepth = 8;
 
-template <class F>
-__device__ __forceinline__ unsigned long long stream_item(const uint32_t *__restrict__ adj,
-                                                          const uint2 *__restrict__ rng,
-                                                          uint32_t k0, uint32_t k1, int lane,
-                                                          F f) {
-    unsigned long long cnt = 0;
+template <bool kSkipIdle, class F>
+__device__ __forceinline__ uint32_t stream_item(const uint32_t *__restrict__ adj,
+                                                const uint2 *__restrict__ rng, uint32_t k0,
+                                                uint32_t k1, int lane, uint32_t idle, F f) {
+    uint32_t cnt = 0;
     uint32_t kb = k0;
     uint32_t nb = min(32u, k1 - kb);
     uint2 my = (kb + lane < k1) ? __ldg(rng + kb + lane) : make_uint2(0u, 0u);
@@ -225,9 +226,9 @@ __device__ __forceinline__ unsigned long long stream_item(const uint32_t *__rest
         }
     };
     auto next_block = [&]() -> uint32_t {
-        if (!live) return kEmpty;
+        if (!live) return idle;
         const uint32_t i = X + lane;
-        const uint32_t w = i < Y ? __ldg(adj + i) : kEmpty;
+        const uint32_t w = i < Y ? __ldg(adj + i) : idle;
         X += 32;
         settle();
         return w;
@@ -240,13 +241,13 @@ __device__ __forceinline__ unsigned long long stream_item(const uint32_t *__rest
 #pragma unroll
         for (int d = 0; d < kDepth; ++d) {
             const uint32_t w = buf[d];
-            if (w != kEmpty) cnt += f(w);
+            if (!kSkipIdle || w != idle) cnt += f(w);
             buf[d] = next_block();
         }
     }
 #pragma unroll
     for (int d = 0; d < kDepth; ++d)
-        if (buf[d] != kEmpty) cnt += f(buf[d]);
+        if (!kSkipIdle || buf[d] != idle) cnt += f(buf[d]);
     return cnt;
 }
 
@@ -258,8 +259,10 @@ __global__ void k_tc_warp(const uint64_t *__restrict__ off, const uint32_t *__re
     extern __shared__ __align__(16) uint32_t smem[];
     __shared__ unsigned long long red[32];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    uint32_t *reg = smem + (size_t)warp * p.R;
-    for (uint32_t q = lane; q < p.R; q += 32) reg[q] = 0u;  // the region is all-zero between items
+    // R words of region + one guard word (reg[R]) that stays zero: idle lanes of the bitmap
+    // test read it instead of branching
+    uint32_t *reg = smem + (size_t)warp * (p.R + 1);
+    for (uint32_t q = lane; q <= p.R; q += 32) reg[q] = 0u;  // all-zero between items
     __syncwarp();
     const uint32_t RB = p.R * 32;  // bitmap capacity in bits
     const unsigned long long nitems = acc[2];
@@ -299,13 +302,14 @@ __global__ void k_tc_warp(const uint64_t *__restrict__ off, const uint32_t *__re
         __syncwarp();
         if (mode == 0) {
             const uint32_t base = v + 1;
-            cnt += stream_item(adj, in_rng + kin, k0, k1, lane, [&](uint32_t w) -> uint32_t {
-                const uint32_t o = w - base;
-                return (reg[o >> 5] >> (o & 31)) & 1u;
-            });
+            cnt += stream_item<false>(adj, in_rng + kin, k0, k1, lane, base + 32 * p.R,
+                                      [&](uint32_t w) -> uint32_t {
+                                          const uint32_t o = w - base;
+                                          return __funnelshift_r(reg[o >> 5], 0u, o) & 1u;
+                                      });
         } else if (mode == 1) {
-            cnt += stream_item(adj, in_rng + kin, k0, k1, lane,
-                               [&](uint32_t w) -> uint32_t { return hash_probe(reg, lg, w); });
+            cnt += stream_item<true>(adj, in_rng + kin, k0, k1, lane, kEmpty,
+                                     [&](uint32_t w) -> uint32_t { return hash_probe(reg, lg, w); });
         } else {
             for (uint32_t kk = k0; kk < k1; ++kk) {
                 const uint2 r = __ldg(in_rng + kin + kk);
@@ -392,7 +396,7 @@ rtg_status batched_shape(rtg_ctx *ctx, const CountCsr &c, const rtg_config &cfg,
     bs->pc.E = cfg.tc_item_edges;
     bs->pc.R = cfg.tc_region_words;
     bs->pc.n = c.n;
-    bs->smem = (size_t)bs->W * bs->pc.R * 4;
+    bs->smem = (size_t)bs->W * (bs->pc.R + 1) * 4;  // region + guard word per warp
     if (bs->smem + 256 > (size_t)ctx->smem_optin)
         return fail(ctx, RTG_ERR_INVALID_ARG, "schedule needs %zu B of shared memory", bs->smem);
     bs->item_cap = c.m / bs->pc.E + c.n + 1;

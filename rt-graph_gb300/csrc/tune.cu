@@ -147,7 +147,7 @@ extern "C" rtg_status rtg_tune_tc(rtg_ctx *ctx, rtg_graph *g, const char *cache_
                 uint64_t got = 0;
                 double ms = 0;
                 res->candidates++;
-                if ((size_t)W * R * 4 + 256 > (size_t)ctx->smem_optin ||
+                if ((size_t)W * (R + 1) * 4 + 256 > (size_t)ctx->smem_optin ||
                     run(c, &got, &ms) != RTG_OK || got != want) {
                     res->rejected++;
                     continue;
