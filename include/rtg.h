@@ -93,9 +93,11 @@ typedef enum rtg_tc_mode { RTG_TC_PLAIN = 0, RTG_TC_BATCHED = 1 } rtg_tc_mode;
 /* Set-intersection execution forms (flags of rtg_si_count*).
  *  AUTO   : BATCHED form — one persistent launch; both lists of every pair (or of every
  *           chunk pair of a long pair) are staged into shared memory by bulk copies and
- *           merged there, several pairs in flight per warp.
- *  PLAIN  : per-pair family from global memory: SEARCH when |long| > si_search_ratio *
- *           |short|, MERGE otherwise.
+ *           merged there, several pairs in flight per warp; a pair longer than a staging
+ *           slot whose long list exceeds si_search_ratio (default 8) x the short one is
+ *           binary-searched from global memory instead.
+ *  PLAIN  : per-pair family from global memory: SEARCH when |long| > si_search_ratio
+ *           (default 32) x |short|, MERGE otherwise.
  *  FORCE_*: one family for every pair; these back the reference's per-baseline CLIs. */
 #define RTG_SI_AUTO 0u
 #define RTG_SI_FORCE_MERGE 1u   /* warp merge path (ip.cu)                        */

@@ -43,7 +43,8 @@ namespace rtg {
 namespace {
 
 constexpr uint32_t kDefaultSiWarps = 8;
-constexpr uint32_t kDefaultSearchRatio = 32;
+constexpr uint32_t kDefaultSearchRatio = 32;  // PLAIN: per-pair MERGE / SEARCH choice
+constexpr uint32_t kDefaultStreamRatio = 8;   // batched: search a pair longer than a slot
 constexpr uint32_t kSiHashSlots = 2048;
 constexpr uint32_t kDefaultStreamWarps = 8;
 constexpr uint32_t kDefaultStageSlots = 2;
@@ -215,6 +216,51 @@ __device__ __forceinline__ uint32_t merge_range_count(const uint32_t *A, uint32_
     return c;
 }
 
+// |A ∩ B| for a short list A against a long list B in global memory. The 32 bucket maxima
+// of B (one per lane, b/32 elements per bucket) locate each A element's bucket with five
+// register shuffles; the element is then binary-searched inside its bucket. Each lane
+// searches kSkewIlp A elements in lockstep so their dependent loads overlap (two keep the
+// kernel at 80 registers, three resident blocks per SM).
+constexpr int kSkewIlp = 2;
+
+__device__ __forceinline__ uint32_t skew_search_count(const uint32_t *__restrict__ A, uint32_t a,
+                                                      const uint32_t *__restrict__ B, uint32_t b,
+                                                      int lane) {
+    const uint32_t step = (b + 31) / 32;
+    const uint32_t first = (uint32_t)lane * step;
+    const uint32_t smp = first < b ? __ldg(B + min(first + step, b) - 1) : kEmpty;
+    const uint32_t iters = 33 - __clz(step);  // lower_bound over step elements converges
+    uint32_t c = 0;
+    for (uint32_t i0 = 0; i0 < a; i0 += 32 * kSkewIlp) {
+        uint32_t x[kSkewIlp], lo[kSkewIlp], hi[kSkewIlp];
+#pragma unroll
+        for (int k = 0; k < kSkewIlp; ++k) {
+            const uint32_t idx = i0 + 32 * k + lane;
+            x[k] = idx < a ? __ldg(A + idx) : kEmpty;
+            uint32_t pos = 0;  // number of bucket maxima below x (at most 31)
+#pragma unroll
+            for (uint32_t st = 16; st; st >>= 1)
+                if (__shfl_sync(kFull, smp, pos + st - 1) < x[k]) pos += st;
+            lo[k] = pos * step;
+            hi[k] = idx < a ? min(lo[k] + step, b) : lo[k];
+        }
+        for (uint32_t it = 0; it < iters; ++it) {
+#pragma unroll
+            for (int k = 0; k < kSkewIlp; ++k) {
+                if (lo[k] < hi[k]) {
+                    const uint32_t mid = (lo[k] + hi[k]) >> 1;
+                    if (__ldg(B + mid) < x[k]) lo[k] = mid + 1;
+                    else hi[k] = mid;
+                }
+            }
+        }
+#pragma unroll
+        for (int k = 0; k < kSkewIlp; ++k)
+            c += (i0 + 32 * k + lane < a && lo[k] < b && __ldg(B + lo[k]) == x[k]) ? 1u : 0u;
+    }
+    return c;
+}
+
 __global__ void k_si_stream(SiArgs s, uint32_t *out, unsigned long long *head, StreamCfg p,
                             uint32_t *status) {
     extern __shared__ __align__(128) unsigned char stage_smem[];
@@ -364,7 +410,7 @@ __global__ void k_si_stream(SiArgs s, uint32_t *out, unsigned long long *head, S
             pk = cur.base + e;
             ++e;
             if (kind == kPairSkewed) {
-                uint32_t c = warp_search_count(LA, a, LB, b, lane);
+                uint32_t c = skew_search_count(LA, a, LB, b, lane);
                 c = __reduce_add_sync(kFull, c);
                 if (lane == 0) out[pk] = c;
                 continue;
@@ -550,7 +596,7 @@ rtg_status si_count_device(rtg_ctx *ctx, const PairSpec &ps, uint32_t *d_out, ui
         sc.S = cf.si_stage_slots ? cf.si_stage_slots : kDefaultStageSlots;
         const uint32_t slot_bytes = cf.si_stage_bytes ? cf.si_stage_bytes : kDefaultStageBytes;
         sc.slot_words = slot_bytes / 4;
-        sc.ratio = ratio;
+        sc.ratio = cf.si_search_ratio ? cf.si_search_ratio : kDefaultStreamRatio;
         sc.meta_off = ((W * sc.S * 8) + 127u) & ~127u;
         sc.cnt_off = (sc.meta_off + W * sc.S * kMetaWords * 4 + 127u) & ~127u;
         sc.ring_off = (sc.cnt_off + W * kMaxSeg * 4 + 127u) & ~127u;

@@ -245,7 +245,7 @@ extern "C" rtg_status rtg_tune_si(rtg_ctx *ctx, const rtg_sets *s, const uint32_
     for (uint32_t B : {2048u, 4096u, 8192u})
         for (uint32_t S : {2u, 3u, 4u})
             for (uint32_t W : {4u, 8u, 16u})
-                for (uint32_t ratio : {16u, 32u, 64u}) {
+                for (uint32_t ratio : {4u, 8u, 16u, 32u}) {
                     rtg_config c = def;
                     c.si_stage_bytes = B;
                     c.si_stage_slots = S;
