@@ -626,6 +626,20 @@ def run_gpu(args, dist: Dist) -> None:
               "roofline": {k: r["roofline"][k] for k in ("achieved", "peak", "unit", "frac",
                                                          "traffic", "kernel")},
               "gpu_launches": r["launches"], "schedule": r["schedule"]["best"]}
+    serving = None
+    if not args.tc_only and not args.no_serve and dist.rank == 0:
+        r = measure_serve(args)
+        mid = next(x for x in r["levels"] if x["load"] == 0.8)
+        serving = {"metric": "serving p99 latency", "value": mid["p99_ms"], "unit": "ms",
+                   "p50_ms": mid["p50_ms"], "at": "load 0.8 of saturation",
+                   "workload": SERVE_WORKLOAD["workload"],
+                   "saturation_requests_per_s": r["saturation"]["requests_per_s"],
+                   "intersections_per_s": mid["intersections_per_s"],
+                   "tc_edges_per_s": mid["tc_edges_per_s"],
+                   "levels": [{k: x[k] for k in ("load", "requests_per_s", "p50_ms", "p99_ms")}
+                              for x in r["levels"]],
+                   "max_requests_per_launch": r["max_requests_per_launch"],
+                   "max_inflight_launches": r["max_inflight_launches"]}
     if dist.rank == 0:
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": dist.ws,
                 "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
@@ -644,7 +658,8 @@ def run_gpu(args, dist: Dist) -> None:
                           "ms_per_step": sum(plain_ms) / len(plain_ms)},
                 "batched_over_plain": value / plain_value,
                 "roofline": roofline, "cpu_baseline": cpu, "clocks": clk.summary(),
-                "gpu_launches": int(launches), "schedule": tune, "si": si}
+                "gpu_launches": int(launches), "schedule": tune, "si": si,
+                "serving": serving}
         print(json.dumps(line), flush=True)
     ctx.close()
 
@@ -660,7 +675,9 @@ def main() -> None:
     ap.add_argument("--workload", default="tc", choices=["tc", "si", "serve"],
                     help="tc: R-MAT-21 triangle count (with a batched-SI summary); "
                          "si: the 1e6-pair batched set intersection alone")
-    ap.add_argument("--tc-only", action="store_true", help="skip the batched-SI summary")
+    ap.add_argument("--tc-only", action="store_true",
+                    help="skip the batched-SI and serving summaries")
+    ap.add_argument("--no-serve", action="store_true", help="skip the serving summary")
     args = ap.parse_args()
     if args.warmup < 3:
         ap.error("at least 3 warm-up steps")
