@@ -62,7 +62,12 @@ typedef struct rtg_sets rtg_sets;
  *             (tc/graph/graph.cpp:23-38).
  *  EDGE_TXT : "src dst" per line, as read by Graph::Txt2Bin (graph.cpp:179-214).
  *  MTX      : MatrixMarket coordinate file, 1-based (bfs/graph/graph.cpp:17-122). */
-typedef enum rtg_format { RTG_FMT_EDGE_BIN = 0, RTG_FMT_EDGE_TXT = 1, RTG_FMT_MTX = 2 } rtg_format;
+typedef enum rtg_format {
+    RTG_FMT_EDGE_BIN = 0,
+    RTG_FMT_EDGE_TXT = 1,
+    RTG_FMT_MTX = 2,
+    RTG_FMT_RTG_CSR = 3 /* CSR cache written by rtg_graph_save (rtg_graph_load only) */
+} rtg_format;
 
 /* CSR kinds built by rtg_csr_build.
  *  DEGREE          : simple undirected graph (self loops and duplicates removed), each
@@ -203,6 +208,12 @@ rtg_status rtg_csr_to_host(rtg_ctx *ctx, const rtg_graph *g, int symmetric, uint
 rtg_status rtg_graph_release_edges(rtg_graph *g);
 /* Device bytes currently held by the graph. */
 uint64_t rtg_graph_device_bytes(const rtg_graph *g);
+/* On-disk CSR cache: write every CSR the graph holds (oriented, counting form, symmetric)
+ * to one file; rtg_graph_load(ctx, path, RTG_FMT_RTG_CSR, &g) reads it back without the
+ * sort-based build (the graph then has no raw edges). A file whose checksum or structure
+ * does not hold is refused with RTG_ERR_FORMAT. No reference counterpart: the reference
+ * rebuilds its CSR (tc/graph/graph.cpp:71-102) on every run. */
+rtg_status rtg_graph_save(rtg_ctx *ctx, const rtg_graph *g, const char *path);
 void rtg_graph_destroy(rtg_graph *g);
 
 /* ------------------------------------------------------ triangle counting */
@@ -373,8 +384,12 @@ const char *rtg_serve_last_error(const rtg_server *s);
  * budget, RTG_ERR_BUSY when every graph slot is taken. */
 rtg_status rtg_serve_add_graph(rtg_server *s, const uint32_t *src, const uint32_t *dst,
                                uint64_t m, uint32_t *graph_id);
+/* With RTG_FMT_RTG_CSR the file must hold the counting form and the symmetric CSR (as
+ * written by rtg_serve_save_graph); nothing is rebuilt. */
 rtg_status rtg_serve_add_graph_file(rtg_server *s, const char *path, rtg_format fmt,
                                     uint32_t *graph_id);
+/* Write a resident graph to a CSR cache file for a later rtg_serve_add_graph_file. */
+rtg_status rtg_serve_save_graph(rtg_server *s, uint32_t graph_id, const char *path);
 /* New requests on the graph are refused at once; it is freed when its last queued or
  * running request completes. */
 rtg_status rtg_serve_remove_graph(rtg_server *s, uint32_t graph_id);

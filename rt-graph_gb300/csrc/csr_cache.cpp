@@ -1,0 +1,289 @@
+// On-disk CSR cache: the CSRs a graph holds on the device (oriented, counting form,
+// symmetric), written to one file and read back without the sort-based build. The layout
+// is this library's own; the CSR arrays are the same ones the reference keeps in
+// Graph::offsets_/adjs_ (tc/graph/graph.cpp:71-102), widened to 64-bit offsets.
+//
+// File (little endian):
+//   char magic[8] = "RTGCSR01"; u32 version = 1; u32 parts (bit 0 oriented, 1 counting,
+//   2 symmetric); u64 m_input; i32 orient; u32 zero;
+//   oriented : u32 n, u32 max_deg, u64 m, u64 work_elems, u32 has_src, u32 zero,
+//              u64 off[n+1], u32 adj[m], (u32 src[m])
+//   counting : u32 n, u32 max_deg, u64 m, u64 off[n+1], u32 adj[m], u64 in_off[n+1],
+//              uint2 in_rng[m]
+//   symmetric: u32 n, u32 max_deg, u64 m, u64 work_elems, u64 off[n+1], u32 adj[m]
+//   u64 fnv1a-64 of every byte after the magic.
+// A file is accepted only if its checksum matches and every array describes a valid CSR
+// (offsets non-decreasing from 0 to m, ids below n, suffix ranges inside their rows), so a
+// damaged or foreign file fails with RTG_ERR_FORMAT before anything reaches a kernel.
+#include <cstdio>
+#include <cstring>
+#include <vector>
+
+#include "internal.h"
+
+namespace rtg {
+namespace {
+
+constexpr char kMagic[8] = {'R', 'T', 'G', 'C', 'S', 'R', '0', '1'};
+constexpr uint32_t kVersion = 1;
+enum : uint32_t { kPartOri = 1, kPartCnt = 2, kPartSym = 4 };
+
+struct Writer {
+    FILE *f;
+    uint64_t h = 1469598103934665603ull;
+    bool ok = true;
+    void put(const void *p, size_t bytes) {
+        if (!ok || bytes == 0) return;
+        const unsigned char *c = static_cast<const unsigned char *>(p);
+        for (size_t i = 0; i < bytes; ++i) h = (h ^ c[i]) * 1099511628211ull;
+        ok = std::fwrite(p, 1, bytes, f) == bytes;
+    }
+    template <class T> void val(T v) { put(&v, sizeof v); }
+};
+
+struct Reader {
+    FILE *f;
+    uint64_t h = 1469598103934665603ull;
+    uint64_t left;
+    bool ok = true;
+    bool get(void *p, size_t bytes) {
+        if (!ok || bytes > left) return ok = false;
+        if (bytes && std::fread(p, 1, bytes, f) != bytes) return ok = false;
+        left -= bytes;
+        const unsigned char *c = static_cast<const unsigned char *>(p);
+        for (size_t i = 0; i < bytes; ++i) h = (h ^ c[i]) * 1099511628211ull;
+        return true;
+    }
+    template <class T> bool val(T &v) { return get(&v, sizeof v); }
+};
+
+template <class T>
+rtg_status to_host(rtg_ctx *ctx, const T *d, uint64_t count, std::vector<T> &h) {
+    h.resize(count ? count : 1);
+    if (count) RTG_CUDA(ctx, cudaMemcpy(h.data(), d, count * sizeof(T), cudaMemcpyDeviceToHost));
+    return RTG_OK;
+}
+
+// offsets non-decreasing from 0 to m
+bool valid_offsets(const std::vector<uint64_t> &off, uint64_t n, uint64_t m) {
+    if (off[0] != 0 || off[n] != m) return false;
+    for (uint64_t v = 0; v < n; ++v)
+        if (off[v + 1] < off[v]) return false;
+    return true;
+}
+
+bool valid_ids(const std::vector<uint32_t> &ids, uint64_t m, uint64_t n) {
+    for (uint64_t i = 0; i < m; ++i)
+        if (ids[i] >= n) return false;
+    return true;
+}
+
+template <class T>
+rtg_status upload(rtg_ctx *ctx, T **d, const std::vector<T> &h, uint64_t count, size_t pad) {
+    RTG_TRY(dev_alloc(ctx, (void **)d, count * sizeof(T) + pad));
+    if (count) RTG_CUDA(ctx, cudaMemcpy(*d, h.data(), count * sizeof(T), cudaMemcpyHostToDevice));
+    if (pad) RTG_CUDA(ctx, cudaMemset((char *)*d + count * sizeof(T), 0, pad));
+    return RTG_OK;
+}
+
+}  // namespace
+}  // namespace rtg
+
+using namespace rtg;
+
+extern "C" rtg_status rtg_graph_save(rtg_ctx *ctx, const rtg_graph *g, const char *path) {
+    if (!ctx || !g || !path) return RTG_ERR_INVALID_ARG;
+    const uint32_t parts = (g->ori.built ? kPartOri : 0) | (g->cnt.built ? kPartCnt : 0) |
+                           (g->sym.built ? kPartSym : 0);
+    if (!parts) return fail(ctx, RTG_ERR_STATE, "graph holds no CSR to save");
+    RTG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    FILE *f = std::fopen(path, "wb");
+    if (!f) return fail(ctx, RTG_ERR_IO, "cannot open %s for writing", path);
+    if (std::fwrite(kMagic, 1, 8, f) != 8) {
+        std::fclose(f);
+        return fail(ctx, RTG_ERR_IO, "write failed: %s", path);
+    }
+    Writer w{f};
+    w.val(kVersion);
+    w.val(parts);
+    w.val(g->m_input);
+    w.val((int32_t)g->orient);
+    w.val((uint32_t)0);
+    std::vector<uint64_t> off;
+    std::vector<uint32_t> adj;
+    rtg_status st = RTG_OK;
+    auto csr = [&](const Csr &c, bool with_src) {
+        w.val(c.n);
+        w.val(c.max_deg);
+        w.val(c.m);
+        w.val(c.work_elems);
+        if (with_src) {
+            w.val((uint32_t)(c.src ? 1 : 0));
+            w.val((uint32_t)0);
+        }
+        if ((st = to_host(ctx, c.off, c.n + 1ull, off)) != RTG_OK) return;
+        w.put(off.data(), (c.n + 1ull) * 8);
+        if ((st = to_host(ctx, c.adj, c.m, adj)) != RTG_OK) return;
+        w.put(adj.data(), c.m * 4);
+        if (with_src && c.src) {
+            if ((st = to_host(ctx, c.src, c.m, adj)) != RTG_OK) return;
+            w.put(adj.data(), c.m * 4);
+        }
+    };
+    if (parts & kPartOri) csr(g->ori, true);
+    if (st == RTG_OK && (parts & kPartCnt)) {
+        const CountCsr &c = g->cnt;
+        w.val(c.n);
+        w.val(c.max_deg);
+        w.val(c.m);
+        std::vector<uint2> rng;
+        if ((st = to_host(ctx, c.off, c.n + 1ull, off)) == RTG_OK) w.put(off.data(), (c.n + 1ull) * 8);
+        if (st == RTG_OK && (st = to_host(ctx, c.adj, c.m, adj)) == RTG_OK) w.put(adj.data(), c.m * 4);
+        if (st == RTG_OK && (st = to_host(ctx, c.in_off, c.n + 1ull, off)) == RTG_OK)
+            w.put(off.data(), (c.n + 1ull) * 8);
+        if (st == RTG_OK && (st = to_host(ctx, c.in_rng, c.m, rng)) == RTG_OK)
+            w.put(rng.data(), c.m * 8);
+    }
+    if (st == RTG_OK && (parts & kPartSym)) csr(g->sym, false);
+    const uint64_t h = w.h;
+    if (st == RTG_OK) w.put(&h, 8);
+    const bool ok = w.ok;
+    if (std::fclose(f) != 0 || !ok) {
+        std::remove(path);
+        return st != RTG_OK ? st : fail(ctx, RTG_ERR_IO, "write failed: %s", path);
+    }
+    if (st != RTG_OK) std::remove(path);
+    return st;
+}
+
+namespace rtg {
+
+// Read a file written by rtg_graph_save into a new graph of ctx (no raw edges).
+rtg_status graph_load_cached(rtg_ctx *ctx, const char *path, rtg_graph **out) {
+    FILE *f = std::fopen(path, "rb");
+    if (!f) return fail(ctx, RTG_ERR_IO, "cannot open %s", path);
+    std::fseek(f, 0, SEEK_END);
+    const long long size = std::ftell(f);
+    std::fseek(f, 0, SEEK_SET);
+    char magic[8] = {};
+    if (size < 8 + 8 || std::fread(magic, 1, 8, f) != 8 || std::memcmp(magic, kMagic, 8)) {
+        std::fclose(f);
+        return fail(ctx, RTG_ERR_FORMAT, "%s is not a CSR cache file", path);
+    }
+    Reader r{f, 1469598103934665603ull, (uint64_t)size - 8 - 8};  // checksum excluded
+    uint32_t version = 0, parts = 0, zero = 0;
+    uint64_t m_input = 0;
+    int32_t orient = -1;
+    r.val(version);
+    r.val(parts);
+    r.val(m_input);
+    r.val(orient);
+    r.val(zero);
+    auto bad = [&](const char *why) {
+        std::fclose(f);
+        return fail(ctx, RTG_ERR_FORMAT, "%s: %s", path, why);
+    };
+    if (!r.ok || version != kVersion || !parts || (parts & ~7u)) return bad("bad header");
+    // every array is read and checked on the host before any device allocation
+    struct HostCsr {
+        uint32_t n = 0, max_deg = 0, has_src = 0;
+        uint64_t m = 0, work = 0;
+        std::vector<uint64_t> off, in_off;
+        std::vector<uint32_t> adj, src;
+        std::vector<uint2> rng;
+    } ho, hc, hs;
+    auto read_csr = [&](HostCsr &c, bool with_src, bool with_work) -> bool {
+        if (!r.val(c.n) || !r.val(c.max_deg) || !r.val(c.m)) return false;
+        if (with_work && !r.val(c.work)) return false;
+        if (with_src && (!r.val(c.has_src) || !r.val(zero))) return false;
+        // sizes must fit what is left of the file before anything is allocated
+        const uint64_t need = (c.n + 1ull) * 8 + c.m * 4 + (c.has_src ? c.m * 4 : 0);
+        if (c.m > r.left || need > r.left) return false;
+        c.off.resize(c.n + 1ull);
+        c.adj.resize(c.m ? c.m : 1);
+        if (!r.get(c.off.data(), (c.n + 1ull) * 8) || !r.get(c.adj.data(), c.m * 4)) return false;
+        if (c.has_src) {
+            c.src.resize(c.m ? c.m : 1);
+            if (!r.get(c.src.data(), c.m * 4)) return false;
+        }
+        return valid_offsets(c.off, c.n, c.m) && valid_ids(c.adj, c.m, c.n) &&
+               (!c.has_src || valid_ids(c.src, c.m, c.n));
+    };
+    if ((parts & kPartOri) && !read_csr(ho, true, true)) return bad("oriented CSR");
+    if (parts & kPartCnt) {
+        if (!read_csr(hc, false, false)) return bad("counting CSR");
+        const uint64_t need = (hc.n + 1ull) * 8 + hc.m * 8;
+        if (need > r.left) return bad("counting CSR");
+        hc.in_off.resize(hc.n + 1ull);
+        hc.rng.resize(hc.m ? hc.m : 1);
+        if (!r.get(hc.in_off.data(), (hc.n + 1ull) * 8) || !r.get(hc.rng.data(), hc.m * 8))
+            return bad("counting CSR");
+        if (!valid_offsets(hc.in_off, hc.n, hc.m)) return bad("counting CSR in-edges");
+        // the batched kernel indexes its per-warp bitmap by (element - v - 1): every row of
+        // v must hold ascending ranks above v, and every suffix range of an in-edge of v
+        // must lie inside one row and hold only ranks above v
+        for (uint64_t v = 0; v < hc.n; ++v)
+            for (uint64_t q = hc.off[v]; q < hc.off[v + 1]; ++q)
+                if (hc.adj[q] <= v || (q > hc.off[v] && hc.adj[q] <= hc.adj[q - 1]))
+                    return bad("counting CSR row order");
+        for (uint64_t v = 0; v < hc.n; ++v)
+            for (uint64_t e = hc.in_off[v]; e < hc.in_off[v + 1]; ++e) {
+                const uint2 rg = hc.rng[e];
+                if (rg.x > rg.y || rg.y > hc.m) return bad("suffix range");
+                if (rg.x == rg.y) continue;
+                // the row u holding position x: last offset <= x
+                uint64_t lo = 0, hi = hc.n;
+                while (lo < hi) {
+                    const uint64_t mid = (lo + hi + 1) >> 1;
+                    if (hc.off[mid] <= rg.x) lo = mid;
+                    else hi = mid - 1;
+                }
+                if (lo >= hc.n || rg.y > hc.off[lo + 1] || hc.adj[rg.x] <= v)
+                    return bad("suffix range");
+            }
+    }
+    if ((parts & kPartSym) && !read_csr(hs, false, true)) return bad("symmetric CSR");
+    uint64_t want = 0, h = r.h;
+    if (!r.ok || r.left != 0 || std::fread(&want, 1, 8, f) != 8 || want != h)
+        return bad("checksum mismatch or trailing bytes");
+    std::fclose(f);
+
+    rtg_graph *g = nullptr;
+    // an empty edge list gives a graph with no raw edges to which the CSRs are attached
+    RTG_TRY(rtg_graph_from_host_edges(ctx, nullptr, nullptr, 0, &g));
+    g->m_input = m_input;
+    g->edges_released = true;
+    g->orient = orient;
+    rtg_status st = RTG_OK;
+    auto up_csr = [&](Csr &c, HostCsr &hcsr) {
+        c.n = hcsr.n;
+        c.m = hcsr.m;
+        c.max_deg = hcsr.max_deg;
+        c.work_elems = hcsr.work;
+        if (st == RTG_OK) st = upload(ctx, &c.off, hcsr.off, hcsr.n + 1ull, 0);
+        if (st == RTG_OK) st = upload(ctx, &c.adj, hcsr.adj, hcsr.m, kAdjPadBytes);
+        if (st == RTG_OK && hcsr.has_src) st = upload(ctx, &c.src, hcsr.src, hcsr.m, 0);
+        c.built = st == RTG_OK;
+    };
+    if (parts & kPartOri) up_csr(g->ori, ho);
+    if (parts & kPartCnt) {
+        CountCsr &c = g->cnt;
+        c.n = hc.n;
+        c.m = hc.m;
+        c.max_deg = hc.max_deg;
+        if (st == RTG_OK) st = upload(ctx, &c.off, hc.off, hc.n + 1ull, 0);
+        if (st == RTG_OK) st = upload(ctx, &c.adj, hc.adj, hc.m, kAdjPadBytes);
+        if (st == RTG_OK) st = upload(ctx, &c.in_off, hc.in_off, hc.n + 1ull, 0);
+        if (st == RTG_OK) st = upload(ctx, &c.in_rng, hc.rng, hc.m, 0);
+        c.built = st == RTG_OK;
+    }
+    if (parts & kPartSym) up_csr(g->sym, hs);
+    if (st != RTG_OK) {
+        rtg_graph_destroy(g);
+        return st;
+    }
+    *out = g;
+    return RTG_OK;
+}
+
+}  // namespace rtg

@@ -131,6 +131,9 @@ void dev_free(void *p);
 rtg_status scratch(rtg_ctx *ctx, int slot, size_t bytes, void **p);
 rtg_status check_status_word(rtg_ctx *ctx);
 
+// CSR cache file (csr_cache.cpp): a new graph of ctx from a file written by rtg_graph_save
+rtg_status graph_load_cached(rtg_ctx *ctx, const char *path, rtg_graph **out);
+
 // CSR builder (csr.cu)
 rtg_status build_csr(rtg_ctx *ctx, rtg_graph *g, rtg_orient orient);
 // counting form (rank relabel + in-edge suffix ranges) of an oriented CSR

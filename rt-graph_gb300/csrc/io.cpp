@@ -121,8 +121,15 @@ rtg_status rtg_edges_read(const char *path, rtg_format fmt, uint64_t *m, uint32_
     return RTG_OK;
 }
 
+extern "C++" {
+namespace rtg {
+rtg_status graph_load_cached(rtg_ctx *ctx, const char *path, rtg_graph **out);  // csr_cache.cpp
+}
+}
+
 rtg_status rtg_graph_load(rtg_ctx *ctx, const char *path, rtg_format fmt, rtg_graph **out) {
     if (!ctx || !path || !out) return RTG_ERR_INVALID_ARG;
+    if (fmt == RTG_FMT_RTG_CSR) return rtg::graph_load_cached(ctx, path, out);
     uint64_t m = 0;
     rtg_status st = rtg_edges_read(path, fmt, &m, nullptr, nullptr);
     if (st != RTG_OK) return st;

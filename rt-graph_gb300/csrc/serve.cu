@@ -714,9 +714,39 @@ rtg_status rtg_serve_add_graph_file(rtg_server *s, const char *path, rtg_format 
         std::lock_guard<std::mutex> bl(s->build_mu);
         rtg_status st = rtg_graph_load(s->build, path, fmt, &g);
         if (st != RTG_OK) return srv_fail(s, st, "graph load: %s", rtg_last_error(s->build));
-        if ((st = build_graph(s, g)) != RTG_OK) return st;
+        if (fmt == RTG_FMT_RTG_CSR) {  // a cached graph is used as it is
+            if (!g->cnt.built || !g->sym.built) {
+                rtg_graph_destroy(g);
+                return srv_fail(s, RTG_ERR_FORMAT,
+                                "%s lacks the counting form or the symmetric CSR", path);
+            }
+        } else if ((st = build_graph(s, g)) != RTG_OK) {
+            return st;
+        }
     }
     return add_built_graph(s, g, graph_id);
+}
+
+rtg_status rtg_serve_save_graph(rtg_server *s, uint32_t graph_id, const char *path) {
+    if (!s || !path) return RTG_ERR_INVALID_ARG;
+    rtg_graph *g = nullptr;
+    {
+        std::lock_guard<std::mutex> lk(s->mu);
+        SGraph *sg = nullptr;
+        RTG_TRY(get_graph(s, graph_id, &sg));
+        g = sg->g;
+        sg->refs++;  // keeps the graph resident while it is written
+    }
+    rtg_status st;
+    {
+        std::lock_guard<std::mutex> bl(s->build_mu);
+        st = rtg_graph_save(s->build, g, path);
+        if (st != RTG_OK) srv_fail(s, st, "graph save: %s", rtg_last_error(s->build));
+    }
+    std::lock_guard<std::mutex> lk(s->mu);
+    s->graphs[graph_id].refs--;
+    s->cv.notify_all();
+    return st;
 }
 
 rtg_status rtg_serve_remove_graph(rtg_server *s, uint32_t graph_id) {

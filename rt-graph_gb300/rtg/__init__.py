@@ -24,7 +24,7 @@ lib = C.CDLL(str(LIB_PATH))
 # ---------------------------------------------------------------- constants
 OK, ERR_INVALID_ARG, ERR_OOM, ERR_IO, ERR_FORMAT, ERR_DEVICE, ERR_TIMEOUT, ERR_CANCELLED, \
     ERR_STATE, ERR_BUSY = range(10)
-FMT_EDGE_BIN, FMT_EDGE_TXT, FMT_MTX = 0, 1, 2
+FMT_EDGE_BIN, FMT_EDGE_TXT, FMT_MTX, FMT_RTG_CSR = 0, 1, 2, 3
 ORIENT_DEGREE, ORIENT_DEGREE_RAW_REF, ORIENT_SYMMETRIC = 0, 1, 2
 TC_PLAIN, TC_BATCHED = 0, 1
 SI_AUTO, SI_MERGE, SI_SEARCH, SI_BITMAP, SI_PLAIN = 0, 1, 2, 3, 4
@@ -133,6 +133,7 @@ _SIGS = {
     "rtg_csr_to_host": (C.c_int, [P, P, C.c_int, P, P]),
     "rtg_graph_release_edges": (C.c_int, [P]),
     "rtg_graph_device_bytes": (C.c_uint64, [P]),
+    "rtg_graph_save": (C.c_int, [P, P, C.c_char_p]),
     "rtg_graph_destroy": (None, [P]),
     "rtg_tc_count": (C.c_int, [P, P, C.c_int, u64p, C.POINTER(Timing)]),
     "rtg_tc_count_host_edges": (C.c_int, [P, P, P, C.c_uint64, C.c_int, C.c_int, u64p,
@@ -160,6 +161,7 @@ _SIGS = {
     "rtg_serve_add_graph": (C.c_int, [P, P, P, C.c_uint64, u32p]),
     "rtg_serve_add_graph_file": (C.c_int, [P, C.c_char_p, C.c_int, u32p]),
     "rtg_serve_remove_graph": (C.c_int, [P, C.c_uint32]),
+    "rtg_serve_save_graph": (C.c_int, [P, C.c_uint32, C.c_char_p]),
     "rtg_serve_graph_info": (C.c_int, [P, C.c_uint32, C.POINTER(GraphInfo)]),
     "rtg_serve_submit_tc": (C.c_int, [P, C.c_uint32, u64p]),
     "rtg_serve_submit_pairs": (C.c_int, [P, C.c_uint32, P, P, C.c_uint64, P, u64p]),
@@ -463,6 +465,10 @@ class Graph:
         self.ctx.check(lib.rtg_graph_info_get(self.h, C.byref(i)))
         return i
 
+    def save(self, path: str) -> None:
+        """Write the graph's CSRs to a cache file (read back with FMT_RTG_CSR)."""
+        self.ctx.check(lib.rtg_graph_save(self.ctx.h, self.h, str(path).encode()), "graph_save")
+
     def tune(self, cache: str | None = None) -> dict:
         """Autotune the batched count's schedule for this graph (set on the context)."""
         r = TuneResult()
@@ -630,6 +636,9 @@ class Server:
         self._check(lib.rtg_serve_add_graph_file(self.h, str(path).encode(), fmt, C.byref(gid)),
                     "serve_add_graph_file")
         return gid.value
+
+    def save_graph(self, gid: int, path: str) -> None:
+        self._check(lib.rtg_serve_save_graph(self.h, gid, str(path).encode()), "serve_save_graph")
 
     def remove_graph(self, gid: int) -> None:
         self._check(lib.rtg_serve_remove_graph(self.h, gid), "serve_remove_graph")
