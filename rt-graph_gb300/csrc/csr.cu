@@ -191,18 +191,26 @@ __global__ void k_ref_keep_flags(const uint64_t *keys, uint64_t m, int B, uint64
     }
 }
 
+// Temporaries of one build step, taken in order from the context's grow-only work slots
+// (one Buffers at a time per context; builds on a context are stream-ordered, so a slot
+// is never reused while earlier work on it is pending).
 struct Buffers {
     rtg_ctx *ctx;
-    std::vector<void *> owned;
-    ~Buffers() {
-        for (void *p : owned) dev_free(p);
-    }
+    int next = 0;
     template <class T>
     rtg_status alloc(T **p, uint64_t count) {
-        void *q = nullptr;
-        RTG_TRY(dev_alloc(ctx, &q, count * sizeof(T)));
-        owned.push_back(q);
-        *p = (T *)q;
+        constexpr int kSlots = sizeof(ctx->work) / sizeof(ctx->work[0]);
+        if (next >= kSlots) return fail(ctx, RTG_ERR_STATE, "builder work slots exhausted");
+        DeviceBuffer &b = ctx->work[next++];
+        const size_t bytes = std::max<size_t>(count * sizeof(T), 256);
+        if (b.bytes < bytes) {
+            dev_free(b.ptr);
+            b.ptr = nullptr;
+            b.bytes = 0;
+            RTG_TRY(dev_alloc(ctx, &b.ptr, bytes));
+            b.bytes = bytes;
+        }
+        *p = (T *)b.ptr;
         return RTG_OK;
     }
 };
@@ -333,6 +341,17 @@ __global__ void k_rank_edge_keys(const uint32_t *src, const uint32_t *adj, uint6
     }
 }
 
+// rank edge keys straight from canonical (min id, max id) keys of the simple graph
+__global__ void k_rank_canon_keys(const uint64_t *ukeys, uint64_t m, int B, const uint32_t *rank,
+                                  uint64_t *keys) {
+    const uint64_t lo_mask = (1ull << B) - 1;
+    GRID_STRIDE(i, m) {
+        const uint64_t k = ukeys[i];
+        const uint32_t a = rank[k >> B], b = rank[k & lo_mask];
+        keys[i] = ((uint64_t)min(a, b) << B) | max(a, b);
+    }
+}
+
 // in-edge keys: head rank in the high word, position of the edge in the low word
 __global__ void k_in_keys(const uint32_t *adj_r, uint64_t m, uint64_t *keys) {
     GRID_STRIDE(e, m) { keys[e] = ((uint64_t)adj_r[e] << 32) | (uint32_t)e; }
@@ -346,18 +365,62 @@ __global__ void k_in_fill(const uint64_t *keys, uint64_t m, const uint64_t *off_
     }
 }
 
-}  // namespace
+// Rows, in-edge suffix ranges and stats of the counting form from its rank edge keys
+// (sorted, unique, mr of them) in ek; `other` is a key buffer of mr entries and src_r one
+// of mr words.
+rtg_status count_tail(rtg_ctx *ctx, CountCsr &cc, uint64_t *ek, uint64_t *other, uint64_t mr,
+                      uint32_t n, int B, uint32_t *src_r) {
+    cc.m = mr;
+    if (mr == 0) {
+        RTG_CUDA(ctx, cudaMemsetAsync(cc.off, 0, (n + 1ull) * 8, ctx->stream));
+        RTG_CUDA(ctx, cudaMemsetAsync(cc.in_off, 0, (n + 1ull) * 8, ctx->stream));
+        cc.built = true;
+        return RTG_OK;
+    }
+    k_csr_fill<<<grid_for(ctx, mr), kThreads, 0, ctx->stream>>>(ek, mr, B, cc.adj, src_r);
+    k_row_offsets<<<grid_for(ctx, n + 1ull), kThreads, 0, ctx->stream>>>(ek, mr, B, n, cc.off);
+    k_in_keys<<<grid_for(ctx, mr), kThreads, 0, ctx->stream>>>(cc.adj, mr, other);
+    ctx->launches += 3;
+    RTG_CUDA(ctx, cudaGetLastError());
+    cub::DoubleBuffer<uint64_t> di(other, ek);
+    RTG_TRY(radix_sort(ctx, di, mr, std::min(64, 32 + B)));
+    k_in_fill<<<grid_for(ctx, mr), kThreads, 0, ctx->stream>>>(di.Current(), mr, cc.off, src_r,
+                                                                cc.in_rng);
+    k_row_offsets<<<grid_for(ctx, n + 1ull), kThreads, 0, ctx->stream>>>(di.Current(), mr, 32, n,
+                                                                          cc.in_off);
+    ctx->launches += 2;
+    RTG_CUDA(ctx, cudaGetLastError());
+    unsigned long long *w = ctx->d_scalars;
+    RTG_CUDA(ctx, cudaMemsetAsync(w, 0, 16, ctx->stream));
+    k_stats<<<grid_for(ctx, n), kThreads, 0, ctx->stream>>>(cc.off, cc.adj, nullptr, mr, n, w,
+                                                             (unsigned int *)(w + 1));
+    ctx->launches++;
+    RTG_CUDA(ctx, cudaGetLastError());
+    unsigned long long h[2];
+    RTG_CUDA(ctx, cudaMemcpyAsync(h, w, 16, cudaMemcpyDeviceToHost, ctx->stream));
+    RTG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    cc.max_deg = (uint32_t)h[1];
+    cc.built = true;
+    return RTG_OK;
+}
 
-rtg_status csr_build_count(rtg_ctx *ctx, const Csr &c, CountCsr &cc) {
+rtg_status count_alloc(rtg_ctx *ctx, CountCsr &cc, uint32_t n, uint64_t m) {
     count_csr_free(cc);
-    const uint64_t m = c.m;
-    const uint32_t n = c.n;
     cc.n = n;
     RTG_TRY(dev_alloc(ctx, (void **)&cc.off, (n + 1ull) * 8));
     RTG_TRY(dev_alloc(ctx, (void **)&cc.in_off, (n + 1ull) * 8));
     RTG_TRY(dev_alloc(ctx, (void **)&cc.adj, m * 4 + kAdjPadBytes));
     RTG_TRY(dev_alloc(ctx, (void **)&cc.in_rng, m * 8 + 16));
     RTG_CUDA(ctx, cudaMemsetAsync((char *)cc.adj + m * 4, 0, kAdjPadBytes, ctx->stream));
+    return RTG_OK;
+}
+
+}  // namespace
+
+rtg_status csr_build_count(rtg_ctx *ctx, const Csr &c, CountCsr &cc) {
+    const uint64_t m = c.m;
+    const uint32_t n = c.n;
+    RTG_TRY(count_alloc(ctx, cc, n, m));
     if (m == 0 || n == 0) {
         RTG_CUDA(ctx, cudaMemsetAsync(cc.off, 0, (n + 1ull) * 8, ctx->stream));
         RTG_CUDA(ctx, cudaMemsetAsync(cc.in_off, 0, (n + 1ull) * 8, ctx->stream));
@@ -409,39 +472,60 @@ rtg_status csr_build_count(rtg_ctx *ctx, const Csr &c, CountCsr &cc) {
         RTG_CUDA(ctx, cudaMemcpy(&last, ek + mu - 1, 8, cudaMemcpyDeviceToHost));
         if (last == sentinel) --mu;
     }
-    const uint64_t mr = (uint64_t)mu;
-    cc.m = mr;
-    if (mr == 0) {
-        RTG_CUDA(ctx, cudaMemsetAsync(cc.off, 0, (n + 1ull) * 8, ctx->stream));
-        RTG_CUDA(ctx, cudaMemsetAsync(cc.in_off, 0, (n + 1ull) * 8, ctx->stream));
-        cc.built = true;
-        return RTG_OK;
+    return count_tail(ctx, cc, ek, other, (uint64_t)mu, n, B, src_r);
+}
+
+rtg_status build_count_direct(rtg_ctx *ctx, rtg_graph *g) {
+    const uint64_t m = g->m_input;
+    tc_plan_free(g->plan_batched);
+    tc_plan_free(g->plan_plain);
+    g->plan_batched = g->plan_plain = nullptr;
+    uint32_t maxid = 0;
+    if (m) {
+        unsigned int *d_mx = (unsigned int *)ctx->d_scalars;
+        RTG_CUDA(ctx, cudaMemsetAsync(d_mx, 0, 4, ctx->stream));
+        k_max_id<<<grid_for(ctx, m), kThreads, 0, ctx->stream>>>(g->d_src, g->d_dst, m, d_mx);
+        ctx->launches++;
+        RTG_CUDA(ctx, cudaGetLastError());
+        RTG_TRY(read_u32(ctx, d_mx, &maxid));
+        if (maxid == kEmpty)
+            return fail(ctx, RTG_ERR_INVALID_ARG, "vertex id 0xFFFFFFFF is reserved");
     }
-    k_csr_fill<<<grid_for(ctx, mr), kThreads, 0, ctx->stream>>>(ek, mr, B, cc.adj, src_r);
-    k_row_offsets<<<grid_for(ctx, n + 1ull), kThreads, 0, ctx->stream>>>(ek, mr, B, n, cc.off);
-    k_in_keys<<<grid_for(ctx, mr), kThreads, 0, ctx->stream>>>(cc.adj, mr, other);
-    ctx->launches += 3;
-    RTG_CUDA(ctx, cudaGetLastError());
-    cub::DoubleBuffer<uint64_t> di(other, ek);
-    RTG_TRY(radix_sort(ctx, di, mr, std::min(64, 32 + B)));
-    k_in_fill<<<grid_for(ctx, mr), kThreads, 0, ctx->stream>>>(di.Current(), mr, cc.off, src_r,
-                                                                cc.in_rng);
-    k_row_offsets<<<grid_for(ctx, n + 1ull), kThreads, 0, ctx->stream>>>(di.Current(), mr, 32, n,
-                                                                          cc.in_off);
+    const uint32_t n = m ? maxid + 1 : 0;
+    const int B = bits_for(maxid + 1ull);
+    Buffers buf{ctx, {}};
+    uint64_t *k0, *k1, *r0, *r1;
+    uint32_t *deg, *rank, *src_r;
+    const uint64_t cap = std::max<uint64_t>(m, 1);
+    RTG_TRY(buf.alloc(&k0, cap));
+    RTG_TRY(buf.alloc(&k1, cap));
+    uint64_t *ukeys = k0;
+    uint64_t mu = 0;
+    if (m) RTG_TRY(simple_keys(ctx, g, maxid, B, k0, k1, &ukeys, &mu));
+    RTG_TRY(count_alloc(ctx, g->cnt, n, mu));
+    if (mu == 0) return count_tail(ctx, g->cnt, nullptr, nullptr, 0, n, B, nullptr);
+    RTG_TRY(buf.alloc(&deg, n));
+    RTG_TRY(buf.alloc(&rank, n));
+    RTG_TRY(buf.alloc(&r0, n));
+    RTG_TRY(buf.alloc(&r1, n));
+    RTG_TRY(buf.alloc(&src_r, mu));
+    // (degree, id) ranks: the degree order of the oriented CSR
+    RTG_CUDA(ctx, cudaMemsetAsync(deg, 0, n * 4ull, ctx->stream));
+    k_degree_from_keys<<<grid_for(ctx, mu), kThreads, 0, ctx->stream>>>(ukeys, mu, B, deg);
+    k_rank_keys<<<grid_for(ctx, n), kThreads, 0, ctx->stream>>>(deg, n, B, r0);
     ctx->launches += 2;
     RTG_CUDA(ctx, cudaGetLastError());
-    unsigned long long *w = ctx->d_scalars;
-    RTG_CUDA(ctx, cudaMemsetAsync(w, 0, 16, ctx->stream));
-    k_stats<<<grid_for(ctx, n), kThreads, 0, ctx->stream>>>(cc.off, cc.adj, nullptr, mr, n, w,
-                                                             (unsigned int *)(w + 1));
-    ctx->launches++;
+    cub::DoubleBuffer<uint64_t> dr(r0, r1);
+    RTG_TRY(radix_sort(ctx, dr, n, std::min(64, B + 32)));
+    k_rank_scatter<<<grid_for(ctx, n), kThreads, 0, ctx->stream>>>(dr.Current(), n, B, rank);
+    uint64_t *other = (ukeys == k0) ? k1 : k0;
+    k_rank_canon_keys<<<grid_for(ctx, mu), kThreads, 0, ctx->stream>>>(ukeys, mu, B, rank, other);
+    ctx->launches += 2;
     RTG_CUDA(ctx, cudaGetLastError());
-    unsigned long long h[2];
-    RTG_CUDA(ctx, cudaMemcpyAsync(h, w, 16, cudaMemcpyDeviceToHost, ctx->stream));
-    RTG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));  // temporaries are freed on return
-    cc.max_deg = (uint32_t)h[1];
-    cc.built = true;
-    return RTG_OK;
+    cub::DoubleBuffer<uint64_t> de(other, ukeys);
+    RTG_TRY(radix_sort(ctx, de, mu, std::min(64, 2 * B)));
+    g->orient = RTG_ORIENT_DEGREE;
+    return count_tail(ctx, g->cnt, de.Current(), de.Alternate(), mu, n, B, src_r);
 }
 
 rtg_status build_csr(rtg_ctx *ctx, rtg_graph *g, rtg_orient orient) {

@@ -77,7 +77,10 @@ struct rtg_ctx {
     unsigned long long *d_scalars = nullptr;  // small device scratch for counters (16 words)
     cudaEvent_t ev[8] = {};
     // grow-only scratch for CUB temp storage and per-call buffers
-    rtg::DeviceBuffer scratch[6];
+    rtg::DeviceBuffer scratch[8];
+    // grow-only temporaries of the CSR builder (kept between builds: no allocation, and
+    // none of the implicit synchronisation of a free, on repeated builds)
+    rtg::DeviceBuffer work[12];
     // graphs and set collections created on this context (released by rtg_destroy)
     std::set<rtg_graph *> graphs;
     std::set<rtg_sets *> sets;
@@ -138,6 +141,9 @@ rtg_status graph_load_cached(rtg_ctx *ctx, const char *path, rtg_graph **out);
 rtg_status build_csr(rtg_ctx *ctx, rtg_graph *g, rtg_orient orient);
 // counting form (rank relabel + in-edge suffix ranges) of an oriented CSR
 rtg_status csr_build_count(rtg_ctx *ctx, const Csr &c, CountCsr &cc);
+// the same counting form straight from g's raw edges (degree order, simple graph), without
+// building the oriented CSR: what a one-shot batched count needs
+rtg_status build_count_direct(rtg_ctx *ctx, rtg_graph *g);
 rtg_status graph_free_csr(Csr &c);
 void count_csr_free(CountCsr &cc);
 

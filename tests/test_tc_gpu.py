@@ -131,6 +131,17 @@ def test_drop_in_host_csr_and_host_edges(ctx):
             assert t.h2d_bytes == 8 * len(s) and t.kernel_launches > 0
 
 
+@pytest.mark.parametrize("name", sorted(TC))
+def test_one_shot_host_edges_all_golden(ctx, name):
+    """rtg_tc_count_host_edges with the degree orientation: the batched form builds the
+    counting form straight from the edges; both forms give the reference's count."""
+    rec = TC[name]
+    s, d = golden_edges(rec)
+    for mode in MODES:
+        got, t = ctx.tc_count_host_edges(s, d, rtg.ORIENT_DEGREE, mode)
+        assert got == rec["triangles"], (name, mode)
+
+
 def test_file_formats(ctx, tmp_path):
     rec = TC["wheel"]
     s, d = golden_edges(rec)
