@@ -341,6 +341,17 @@ __global__ void k_rank_edge_keys(const uint32_t *src, const uint32_t *adj, uint6
     }
 }
 
+// degrees of the simple graph from its sorted canonical keys: the row length of the
+// smaller endpoint (offsets of the sorted keys, no atomics on the hub rows) ...
+__global__ void k_degree_lo(const uint64_t *off_lo, uint32_t n, uint32_t *deg) {
+    GRID_STRIDE(v, (uint64_t)n) { deg[v] = (uint32_t)(off_lo[v + 1] - off_lo[v]); }
+}
+// ... plus one per key for the larger endpoint
+__global__ void k_degree_hi(const uint64_t *keys, uint64_t m, int B, uint32_t *deg) {
+    const uint64_t lo_mask = (1ull << B) - 1;
+    GRID_STRIDE(i, m) { atomicAdd(&deg[keys[i] & lo_mask], 1u); }
+}
+
 // rank edge keys straight from canonical (min id, max id) keys of the simple graph
 __global__ void k_rank_canon_keys(const uint64_t *ukeys, uint64_t m, int B, const uint32_t *rank,
                                   uint64_t *keys) {
@@ -352,16 +363,33 @@ __global__ void k_rank_canon_keys(const uint64_t *ukeys, uint64_t m, int B, cons
     }
 }
 
-// in-edge keys: head rank in the high word, position of the edge in the low word
-__global__ void k_in_keys(const uint32_t *adj_r, uint64_t m, uint64_t *keys) {
-    GRID_STRIDE(e, m) { keys[e] = ((uint64_t)adj_r[e] << 32) | (uint32_t)e; }
+// in-edges: (head rank, position) pairs, grouped by a stable 32-bit key sort so positions
+// stay ascending within a head
+__global__ void k_in_pairs(const uint32_t *adj_r, uint64_t m, uint32_t *keys, uint32_t *pos) {
+    GRID_STRIDE(e, m) {
+        keys[e] = adj_r[e];
+        pos[e] = (uint32_t)e;
+    }
 }
 
-__global__ void k_in_fill(const uint64_t *keys, uint64_t m, const uint64_t *off_r,
+__global__ void k_in_fill(const uint32_t *pos, uint64_t m, const uint64_t *off_r,
                           const uint32_t *src_r, uint2 *rng) {
     GRID_STRIDE(i, m) {
-        const uint32_t e = (uint32_t)keys[i];
+        const uint32_t e = pos[i];
         rng[i] = make_uint2(e + 1, (uint32_t)off_r[src_r[e] + 1]);
+    }
+}
+
+// row offsets of sorted 32-bit keys: off[x] = first i with keys[i] >= x
+__global__ void k_row_offsets32(const uint32_t *keys, uint64_t m, uint32_t n, uint64_t *off) {
+    GRID_STRIDE(x, (uint64_t)n + 1) {
+        uint64_t lo = 0, hi = m;
+        while (lo < hi) {
+            const uint64_t mid = (lo + hi) >> 1;
+            if (keys[mid] < x) lo = mid + 1;
+            else hi = mid;
+        }
+        off[x] = lo;
     }
 }
 
@@ -379,15 +407,25 @@ rtg_status count_tail(rtg_ctx *ctx, CountCsr &cc, uint64_t *ek, uint64_t *other,
     }
     k_csr_fill<<<grid_for(ctx, mr), kThreads, 0, ctx->stream>>>(ek, mr, B, cc.adj, src_r);
     k_row_offsets<<<grid_for(ctx, n + 1ull), kThreads, 0, ctx->stream>>>(ek, mr, B, n, cc.off);
-    k_in_keys<<<grid_for(ctx, mr), kThreads, 0, ctx->stream>>>(cc.adj, mr, other);
+    // ek is free once rows are filled: the pair sort ping-pongs between `other` and ek
+    uint32_t *ka = reinterpret_cast<uint32_t *>(other), *pa = ka + mr;
+    uint32_t *kb = reinterpret_cast<uint32_t *>(ek), *pb = kb + mr;
+    k_in_pairs<<<grid_for(ctx, mr), kThreads, 0, ctx->stream>>>(cc.adj, mr, ka, pa);
     ctx->launches += 3;
     RTG_CUDA(ctx, cudaGetLastError());
-    cub::DoubleBuffer<uint64_t> di(other, ek);
-    RTG_TRY(radix_sort(ctx, di, mr, std::min(64, 32 + B)));
-    k_in_fill<<<grid_for(ctx, mr), kThreads, 0, ctx->stream>>>(di.Current(), mr, cc.off, src_r,
+    cub::DoubleBuffer<uint32_t> dk(ka, kb), dv(pa, pb);
+    size_t bytes = 0;
+    RTG_CUDA(ctx, cub::DeviceRadixSort::SortPairs(nullptr, bytes, dk, dv, (int64_t)mr, 0, B,
+                                                  ctx->stream));
+    void *tmp = nullptr;
+    RTG_TRY(scratch(ctx, 0, bytes, &tmp));
+    RTG_CUDA(ctx, cub::DeviceRadixSort::SortPairs(tmp, bytes, dk, dv, (int64_t)mr, 0, B,
+                                                  ctx->stream));
+    ctx->launches += (B + 7) / 8 + 1;
+    k_in_fill<<<grid_for(ctx, mr), kThreads, 0, ctx->stream>>>(dv.Current(), mr, cc.off, src_r,
                                                                 cc.in_rng);
-    k_row_offsets<<<grid_for(ctx, n + 1ull), kThreads, 0, ctx->stream>>>(di.Current(), mr, 32, n,
-                                                                          cc.in_off);
+    k_row_offsets32<<<grid_for(ctx, n + 1ull), kThreads, 0, ctx->stream>>>(dk.Current(), mr, n,
+                                                                            cc.in_off);
     ctx->launches += 2;
     RTG_CUDA(ctx, cudaGetLastError());
     unsigned long long *w = ctx->d_scalars;
@@ -506,14 +544,17 @@ rtg_status build_count_direct(rtg_ctx *ctx, rtg_graph *g) {
     if (mu == 0) return count_tail(ctx, g->cnt, nullptr, nullptr, 0, n, B, nullptr);
     RTG_TRY(buf.alloc(&deg, n));
     RTG_TRY(buf.alloc(&rank, n));
-    RTG_TRY(buf.alloc(&r0, n));
-    RTG_TRY(buf.alloc(&r1, n));
+    RTG_TRY(buf.alloc(&r0, n + 1ull));
+    RTG_TRY(buf.alloc(&r1, n + 1ull));
     RTG_TRY(buf.alloc(&src_r, mu));
-    // (degree, id) ranks: the degree order of the oriented CSR
-    RTG_CUDA(ctx, cudaMemsetAsync(deg, 0, n * 4ull, ctx->stream));
-    k_degree_from_keys<<<grid_for(ctx, mu), kThreads, 0, ctx->stream>>>(ukeys, mu, B, deg);
+    // (degree, id) ranks: the degree order of the oriented CSR. The keys are sorted by
+    // their smaller endpoint, so its share of the degree is a row length (r0 holds the
+    // row offsets for a moment); the larger endpoint's share is counted with atomics.
+    k_row_offsets<<<grid_for(ctx, n + 1ull), kThreads, 0, ctx->stream>>>(ukeys, mu, B, n, r0);
+    k_degree_lo<<<grid_for(ctx, n), kThreads, 0, ctx->stream>>>(r0, n, deg);
+    k_degree_hi<<<grid_for(ctx, mu), kThreads, 0, ctx->stream>>>(ukeys, mu, B, deg);
     k_rank_keys<<<grid_for(ctx, n), kThreads, 0, ctx->stream>>>(deg, n, B, r0);
-    ctx->launches += 2;
+    ctx->launches += 4;
     RTG_CUDA(ctx, cudaGetLastError());
     cub::DoubleBuffer<uint64_t> dr(r0, r1);
     RTG_TRY(radix_sort(ctx, dr, n, std::min(64, B + 32)));
