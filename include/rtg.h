@@ -221,7 +221,10 @@ void rtg_graph_destroy(rtg_graph *g);
 rtg_status rtg_tc_count(rtg_ctx *ctx, rtg_graph *g, rtg_tc_mode mode, uint64_t *out_total,
                         rtg_timing *timing);
 /* End to end from host edges: copy in, build the CSR with `orient`, count, copy the
- * total out. The drop-in for the bs_tc / rt_tc pipelines. */
+ * total out. The drop-in for the bs_tc / rt_tc pipelines. With RTG_ORIENT_DEGREE and
+ * RTG_TC_BATCHED the edges, the counting form and the count's buffers are kept in the
+ * context's grow-only scratch (about 21 bytes per edge, released by rtg_destroy), so
+ * repeated calls allocate nothing once it has grown. */
 rtg_status rtg_tc_count_host_edges(rtg_ctx *ctx, const uint32_t *src, const uint32_t *dst,
                                    uint64_t m, rtg_orient orient, rtg_tc_mode mode,
                                    uint64_t *out_total, rtg_timing *timing);

@@ -561,14 +561,26 @@ rtg_status rtg_tc_count_host_edges(rtg_ctx *ctx, const uint32_t *src, const uint
     rtg_timing t{};
     double t0 = now_ms();
     uint64_t l0 = ctx->launches;
-    rtg_graph *g = nullptr;
-    RTG_CUDA(ctx, cudaEventRecord(ctx->ev[6], ctx->stream));
-    RTG_TRY(rtg_graph_from_host_edges(ctx, src, dst, m, &g));
-    RTG_CUDA(ctx, cudaEventRecord(ctx->ev[7], ctx->stream));
     if (mode == RTG_TC_BATCHED && orient == RTG_ORIENT_DEGREE) {
         // one-shot batched count: the counting form is built straight from the edges (no
-        // oriented CSR) and counted with direct launches into context scratch (no plan)
-        rtg_status s = build_count_direct(ctx, g);
+        // oriented CSR) and counted with direct launches (no plan); the edges, the counting
+        // form and the count's buffers live in grow-only context scratch, so repeated calls
+        // allocate and free nothing. The graph object is local and only borrows them.
+        rtg_graph tg;
+        rtg_graph *g = &tg;
+        void *pe = nullptr;
+        const uint64_t mpad = (m + 63) & ~63ull;
+        RTG_CUDA(ctx, cudaEventRecord(ctx->ev[6], ctx->stream));
+        RTG_TRY(scratch(ctx, 2, mpad * 8 + 256, &pe));
+        tg.d_src = static_cast<uint32_t *>(pe);
+        tg.d_dst = tg.d_src + mpad;
+        tg.m_input = m;
+        if (m) {
+            RTG_CUDA(ctx, cudaMemcpyAsync(tg.d_src, src, m * 4, cudaMemcpyHostToDevice, ctx->stream));
+            RTG_CUDA(ctx, cudaMemcpyAsync(tg.d_dst, dst, m * 4, cudaMemcpyHostToDevice, ctx->stream));
+        }
+        RTG_CUDA(ctx, cudaEventRecord(ctx->ev[7], ctx->stream));
+        rtg_status s = build_count_direct(ctx, g, true);
         void *scr = nullptr;
         const uint64_t need = s == RTG_OK ? tc_plan_estimate_bytes(ctx, g) : 0;
         if (s == RTG_OK) s = scratch(ctx, 6, need, &scr);
@@ -590,7 +602,8 @@ rtg_status rtg_tc_count_host_edges(rtg_ctx *ctx, const uint32_t *src, const uint
             if (e != cudaSuccess) s = cuda_fail(ctx, e, "count", __FILE__, __LINE__);
         }
         if (s == RTG_OK) s = check_status_word(ctx);
-        rtg_graph_destroy(g);
+        tg.d_src = tg.d_dst = nullptr;  // borrowed scratch: nothing here is freed
+        tg.cnt = CountCsr{};
         if (s != RTG_OK) return s;
         float ms = 0;
         cudaEventElapsedTime(&ms, ctx->ev[0], ctx->ev[1]);
@@ -602,6 +615,10 @@ rtg_status rtg_tc_count_host_edges(rtg_ctx *ctx, const uint32_t *src, const uint
         if (timing) *timing = t;
         return RTG_OK;
     }
+    rtg_graph *g = nullptr;
+    RTG_CUDA(ctx, cudaEventRecord(ctx->ev[6], ctx->stream));
+    RTG_TRY(rtg_graph_from_host_edges(ctx, src, dst, m, &g));
+    RTG_CUDA(ctx, cudaEventRecord(ctx->ev[7], ctx->stream));
     rtg_status s = rtg_csr_build(ctx, g, orient);
     if (s == RTG_OK) {
         float h2d = 0;

@@ -453,6 +453,26 @@ rtg_status count_alloc(rtg_ctx *ctx, CountCsr &cc, uint32_t n, uint64_t m) {
     return RTG_OK;
 }
 
+// The same arrays carved from the context's scratch slot kCountScratch (a one-shot count
+// whose graph dies with the call; the caller detaches them before destroying the graph).
+constexpr int kCountScratch = 7;
+
+rtg_status count_alloc_scratch(rtg_ctx *ctx, CountCsr &cc, uint32_t n, uint64_t m) {
+    auto up = [](uint64_t b) { return (b + 255) & ~255ull; };
+    const uint64_t b_off = up((n + 1ull) * 8), b_adj = up(m * 4 + kAdjPadBytes),
+                   b_rng = up(m * 8 + 16);
+    void *p = nullptr;
+    RTG_TRY(scratch(ctx, kCountScratch, 2 * b_off + b_adj + b_rng, &p));
+    char *c = static_cast<char *>(p);
+    cc.n = n;
+    cc.off = reinterpret_cast<uint64_t *>(c);
+    cc.in_off = reinterpret_cast<uint64_t *>(c + b_off);
+    cc.adj = reinterpret_cast<uint32_t *>(c + 2 * b_off);
+    cc.in_rng = reinterpret_cast<uint2 *>(c + 2 * b_off + b_adj);
+    RTG_CUDA(ctx, cudaMemsetAsync((char *)cc.adj + m * 4, 0, kAdjPadBytes, ctx->stream));
+    return RTG_OK;
+}
+
 }  // namespace
 
 rtg_status csr_build_count(rtg_ctx *ctx, const Csr &c, CountCsr &cc) {
@@ -513,7 +533,7 @@ rtg_status csr_build_count(rtg_ctx *ctx, const Csr &c, CountCsr &cc) {
     return count_tail(ctx, cc, ek, other, (uint64_t)mu, n, B, src_r);
 }
 
-rtg_status build_count_direct(rtg_ctx *ctx, rtg_graph *g) {
+rtg_status build_count_direct(rtg_ctx *ctx, rtg_graph *g, bool in_scratch) {
     const uint64_t m = g->m_input;
     tc_plan_free(g->plan_batched);
     tc_plan_free(g->plan_plain);
@@ -540,7 +560,7 @@ rtg_status build_count_direct(rtg_ctx *ctx, rtg_graph *g) {
     uint64_t *ukeys = k0;
     uint64_t mu = 0;
     if (m) RTG_TRY(simple_keys(ctx, g, maxid, B, k0, k1, &ukeys, &mu));
-    RTG_TRY(count_alloc(ctx, g->cnt, n, mu));
+    RTG_TRY(in_scratch ? count_alloc_scratch(ctx, g->cnt, n, mu) : count_alloc(ctx, g->cnt, n, mu));
     if (mu == 0) return count_tail(ctx, g->cnt, nullptr, nullptr, 0, n, B, nullptr);
     RTG_TRY(buf.alloc(&deg, n));
     RTG_TRY(buf.alloc(&rank, n));

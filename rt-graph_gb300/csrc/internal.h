@@ -143,7 +143,9 @@ rtg_status build_csr(rtg_ctx *ctx, rtg_graph *g, rtg_orient orient);
 rtg_status csr_build_count(rtg_ctx *ctx, const Csr &c, CountCsr &cc);
 // the same counting form straight from g's raw edges (degree order, simple graph), without
 // building the oriented CSR: what a one-shot batched count needs
-rtg_status build_count_direct(rtg_ctx *ctx, rtg_graph *g);
+// With in_scratch the counting form's arrays live in a context scratch slot (reused by the
+// next such build); the caller must detach them (null the pointers) before the graph dies.
+rtg_status build_count_direct(rtg_ctx *ctx, rtg_graph *g, bool in_scratch = false);
 rtg_status graph_free_csr(Csr &c);
 void count_csr_free(CountCsr &cc);
 
