@@ -580,7 +580,7 @@ rtg_status rtg_tc_count_host_edges(rtg_ctx *ctx, const uint32_t *src, const uint
             RTG_CUDA(ctx, cudaMemcpyAsync(tg.d_dst, dst, m * 4, cudaMemcpyHostToDevice, ctx->stream));
         }
         RTG_CUDA(ctx, cudaEventRecord(ctx->ev[7], ctx->stream));
-        rtg_status s = build_count_direct(ctx, g, true);
+        rtg_status s = build_count_direct(ctx, g, true, true);
         void *scr = nullptr;
         const uint64_t need = s == RTG_OK ? tc_plan_estimate_bytes(ctx, g) : 0;
         if (s == RTG_OK) s = scratch(ctx, 6, need, &scr);

@@ -341,6 +341,14 @@ __global__ void k_rank_edge_keys(const uint32_t *src, const uint32_t *adj, uint6
     }
 }
 
+// degrees on the raw edge list (duplicates and self loops included)
+__global__ void k_degree_raw(const uint32_t *s, const uint32_t *d, uint64_t m, uint32_t *deg) {
+    GRID_STRIDE(i, m) {
+        atomicAdd(&deg[s[i]], 1u);
+        atomicAdd(&deg[d[i]], 1u);
+    }
+}
+
 // degrees of the simple graph from its sorted canonical keys: the row length of the
 // smaller endpoint (offsets of the sorted keys, no atomics on the hub rows) ...
 __global__ void k_degree_lo(const uint64_t *off_lo, uint32_t n, uint32_t *deg) {
@@ -533,7 +541,7 @@ rtg_status csr_build_count(rtg_ctx *ctx, const Csr &c, CountCsr &cc) {
     return count_tail(ctx, cc, ek, other, (uint64_t)mu, n, B, src_r);
 }
 
-rtg_status build_count_direct(rtg_ctx *ctx, rtg_graph *g, bool in_scratch) {
+rtg_status build_count_direct(rtg_ctx *ctx, rtg_graph *g, bool in_scratch, bool raw_degree) {
     const uint64_t m = g->m_input;
     tc_plan_free(g->plan_batched);
     tc_plan_free(g->plan_plain);
@@ -557,6 +565,52 @@ rtg_status build_count_direct(rtg_ctx *ctx, rtg_graph *g, bool in_scratch) {
     const uint64_t cap = std::max<uint64_t>(m, 1);
     RTG_TRY(buf.alloc(&k0, cap));
     RTG_TRY(buf.alloc(&k1, cap));
+    if (raw_degree && m) {
+        // ranks by degree in the input list (duplicates and self loops counted); the one
+        // sort of the rank edge keys then also brings duplicates together for Unique
+        RTG_TRY(buf.alloc(&deg, n));
+        RTG_TRY(buf.alloc(&rank, n));
+        RTG_TRY(buf.alloc(&r0, n + 1ull));
+        RTG_TRY(buf.alloc(&r1, n + 1ull));
+        RTG_TRY(buf.alloc(&src_r, m));
+        RTG_CUDA(ctx, cudaMemsetAsync(deg, 0, n * 4ull, ctx->stream));
+        k_degree_raw<<<grid_for(ctx, m), kThreads, 0, ctx->stream>>>(g->d_src, g->d_dst, m, deg);
+        k_rank_keys<<<grid_for(ctx, n), kThreads, 0, ctx->stream>>>(deg, n, B, r0);
+        ctx->launches += 2;
+        RTG_CUDA(ctx, cudaGetLastError());
+        cub::DoubleBuffer<uint64_t> dr(r0, r1);
+        RTG_TRY(radix_sort(ctx, dr, n, std::min(64, B + 32)));
+        const uint64_t sentinel = (uint64_t)n << B;
+        k_rank_scatter<<<grid_for(ctx, n), kThreads, 0, ctx->stream>>>(dr.Current(), n, B, rank);
+        k_rank_edge_keys<<<grid_for(ctx, m), kThreads, 0, ctx->stream>>>(g->d_src, g->d_dst, m,
+                                                                          rank, B, sentinel, k0);
+        ctx->launches += 2;
+        RTG_CUDA(ctx, cudaGetLastError());
+        cub::DoubleBuffer<uint64_t> de(k0, k1);
+        RTG_TRY(radix_sort(ctx, de, m, std::min(64, 2 * B)));  // n < 2^B: the sentinel fits
+        int64_t *d_num = (int64_t *)(ctx->d_scalars + 4);
+        size_t bytes = 0;
+        RTG_CUDA(ctx, cub::DeviceSelect::Unique(nullptr, bytes, de.Current(), de.Alternate(),
+                                                d_num, (int64_t)m, ctx->stream));
+        void *tmp = nullptr;
+        RTG_TRY(scratch(ctx, 0, bytes, &tmp));
+        RTG_CUDA(ctx, cub::DeviceSelect::Unique(tmp, bytes, de.Current(), de.Alternate(), d_num,
+                                                (int64_t)m, ctx->stream));
+        ctx->launches += 2;
+        int64_t nu = 0;
+        RTG_CUDA(ctx, cudaMemcpyAsync(&nu, d_num, 8, cudaMemcpyDeviceToHost, ctx->stream));
+        RTG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+        uint64_t *ek = de.Alternate(), *other = de.Current();
+        if (nu > 0) {
+            uint64_t last = 0;
+            RTG_CUDA(ctx, cudaMemcpy(&last, ek + nu - 1, 8, cudaMemcpyDeviceToHost));
+            if (last == sentinel) --nu;
+        }
+        RTG_TRY(in_scratch ? count_alloc_scratch(ctx, g->cnt, n, (uint64_t)nu)
+                           : count_alloc(ctx, g->cnt, n, (uint64_t)nu));
+        g->orient = RTG_ORIENT_DEGREE;
+        return count_tail(ctx, g->cnt, ek, other, (uint64_t)nu, n, B, src_r);
+    }
     uint64_t *ukeys = k0;
     uint64_t mu = 0;
     if (m) RTG_TRY(simple_keys(ctx, g, maxid, B, k0, k1, &ukeys, &mu));

@@ -145,7 +145,11 @@ rtg_status csr_build_count(rtg_ctx *ctx, const Csr &c, CountCsr &cc);
 // building the oriented CSR: what a one-shot batched count needs
 // With in_scratch the counting form's arrays live in a context scratch slot (reused by the
 // next such build); the caller must detach them (null the pointers) before the graph dies.
-rtg_status build_count_direct(rtg_ctx *ctx, rtg_graph *g, bool in_scratch = false);
+// With raw_degree vertices are ranked by their degree in the input list (duplicates and
+// self loops counted), which saves the sort that removes duplicates before ranking: a
+// different orientation of the same simple graph, so the same triangle total.
+rtg_status build_count_direct(rtg_ctx *ctx, rtg_graph *g, bool in_scratch = false,
+                              bool raw_degree = false);
 rtg_status graph_free_csr(Csr &c);
 void count_csr_free(CountCsr &cc);
 
