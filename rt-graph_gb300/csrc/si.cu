@@ -179,12 +179,28 @@ struct StreamCfg {
 
 // Per-slot job description in shared memory (32-bit words):
 //   [0] segments, [1] job kind, [2..3] output index of segment 0's pair (u64), [4] total
-//   merged length L, [kP + s] first diagonal of segment s (kP + nseg holds L),
-//   [kOffA + s] / [kLenA + s] / [kOffB + s] / [kLenB + s] word offset in the slot and length
-//   of the segment's two lists, [kOut + s] output index of segment s relative to [2..3].
+//   merged length L of the merged segments, [5] total short-list length LS of the searched
+//   segments, [kP + s] first diagonal of segment s among the merged ones (kP + nseg holds
+//   L), [kS + s] first short-list element of segment s among the searched ones (kS + nseg
+//   holds LS), [kOffA + s] / [kLenA + s] / [kOffB + s] / [kLenB + s] word offset in the slot
+//   and length of the segment's two lists, [kOut + s] output index of segment s relative
+//   to [2..3]. A segment is merged or searched, never both (its other length is 0).
 constexpr uint32_t kMaxSeg = 16;
-constexpr uint32_t kP = 8, kOffA = 32, kLenA = 48, kOffB = 64, kLenB = 80, kOut = 96;
-constexpr uint32_t kMetaWords = 112;
+constexpr uint32_t kP = 8, kS = 25, kOffA = 48, kLenA = 64, kOffB = 80, kLenB = 96, kOut = 112;
+constexpr uint32_t kMetaWords = 128;
+
+// Number of elements of the sorted list B (nb >= 1, B[nb] = kEmpty) below x: branch-free
+// lower bound over shared memory.
+__device__ __forceinline__ uint32_t smem_lower_bound(const uint32_t *B, uint32_t nb, uint32_t x) {
+    const uint32_t *first = B;
+    uint32_t len = nb;
+    while (len > 1) {
+        const uint32_t half = len >> 1;
+        first = (first[half - 1] < x) ? first + half : first;
+        len -= half;
+    }
+    return (uint32_t)(first - B) + ((*first < x) ? 1u : 0u);
+}
 enum : uint32_t { kJobPacked = 0, kJobChunk = 1, kJobChunkLast = 2 };
 enum : uint32_t { kPairZero = 0, kPairPacked = 1, kPairChunked = 2, kPairSkewed = 3 };
 
@@ -278,12 +294,13 @@ __global__ void k_si_stream(SiArgs s, uint32_t *out, unsigned long long *head, S
     const uint32_t CAPE = p.slot_words - 16;  // list elements per chunk job (room for alignment)
 
     // One batch of 32 pairs, lane e holding pair base + e: its lists, its kind, the words
-    // its widened lists take in a slot and inclusive warp scans of those words and of the
-    // merged lengths of packed pairs.
+    // its widened lists take in a slot and inclusive warp scans of those words, of the
+    // merged lengths of packed pairs that are merged and of the short-list lengths of
+    // packed pairs that are searched (|B| > ratio * |A|: binary search in the slot).
     struct Batch {
         unsigned long long base;
         PairRef r;
-        uint32_t kind, w, sw, sl;
+        uint32_t kind, w, sw, sl, ss;
     };
     auto fetch = [&](Batch &bt) {
         unsigned long long b0 = 0;
@@ -298,17 +315,19 @@ __global__ void k_si_stream(SiArgs s, uint32_t *out, unsigned long long *head, S
         }
         bt.kind = kPairZero;
         bt.w = 0;
-        uint32_t len = 0;
+        uint32_t len = 0, slen = 0;
         if (bt.r.valid && bt.r.a > 0) {
             // words reserved in a slot: each widened list plus one word for its sentinel
             const uint32_t hA = (uint32_t)(reinterpret_cast<uintptr_t>(bt.r.A) & 15u) >> 2;
             const uint32_t hB = (uint32_t)(reinterpret_cast<uintptr_t>(bt.r.B) & 15u) >> 2;
             const uint64_t ww = (((uint64_t)hA + bt.r.a + 4) & ~3ull) + (((uint64_t)hB + bt.r.b + 4) & ~3ull);
+            const bool skew = (uint64_t)bt.r.b > (uint64_t)p.ratio * bt.r.a;
             if (ww <= p.slot_words) {
                 bt.kind = kPairPacked;
                 bt.w = (uint32_t)ww;
-                len = bt.r.a + bt.r.b;
-            } else if ((uint64_t)bt.r.b > (uint64_t)p.ratio * bt.r.a) {
+                if (skew) slen = bt.r.a;
+                else len = bt.r.a + bt.r.b;
+            } else if (skew) {
                 bt.kind = kPairSkewed;
             } else {
                 bt.kind = kPairChunked;
@@ -316,12 +335,15 @@ __global__ void k_si_stream(SiArgs s, uint32_t *out, unsigned long long *head, S
         }
         bt.sw = bt.w;
         bt.sl = len;
+        bt.ss = slen;
 #pragma unroll
         for (int o = 1; o < 32; o <<= 1) {
             const uint32_t x = __shfl_up_sync(kFull, bt.sw, o), y = __shfl_up_sync(kFull, bt.sl, o);
+            const uint32_t z = __shfl_up_sync(kFull, bt.ss, o);
             if (lane >= o) {
                 bt.sw += x;
                 bt.sl += y;
+                bt.ss += z;
             }
         }
     };
@@ -356,6 +378,7 @@ __global__ void k_si_stream(SiArgs s, uint32_t *out, unsigned long long *head, S
                 // consecutive packed (and empty) pairs e .. e1-1 that fit one slot together
                 const uint32_t baseW = e ? __shfl_sync(kFull, cur.sw, e - 1) : 0u;
                 const uint32_t baseL = e ? __shfl_sync(kFull, cur.sl, e - 1) : 0u;
+                const uint32_t baseS = e ? __shfl_sync(kFull, cur.ss, e - 1) : 0u;
                 const uint32_t me = (uint32_t)lane;
                 const bool brk = me > e && (me >= nbat || cur.kind == kPairChunked ||
                                             cur.kind == kPairSkewed || cur.sw - baseW > p.slot_words ||
@@ -364,18 +387,21 @@ __global__ void k_si_stream(SiArgs s, uint32_t *out, unsigned long long *head, S
                 const uint32_t e1 = bm ? (uint32_t)(__ffs(bm) - 1) : 32u;
                 const uint32_t nseg = e1 - e;
                 const uint32_t L = __shfl_sync(kFull, cur.sl, e1 - 1) - baseL;
+                const uint32_t LS = __shfl_sync(kFull, cur.ss, e1 - 1) - baseS;
                 const bool mine = me >= e && me < e1;
                 const bool copies = mine && cur.kind == kPairPacked;
                 uint32_t dst = 0, hA = 0, hB = 0, wa = 0, ca = 0, cb = 0;
                 if (mine) {
                     const uint32_t sg = me - e;
+                    const bool srch = copies && (uint64_t)cur.r.b > (uint64_t)p.ratio * cur.r.a;
                     dst = cur.sw - cur.w - baseW;
                     hA = (uint32_t)(reinterpret_cast<uintptr_t>(cur.r.A) & 15u) >> 2;
                     hB = (uint32_t)(reinterpret_cast<uintptr_t>(cur.r.B) & 15u) >> 2;
                     wa = (hA + cur.r.a + 4) & ~3u;  // A's words + sentinel, 16-byte multiple
                     ca = copies ? (hA + cur.r.a + 3) & ~3u : 0u;  // words copied
                     cb = copies ? (hB + cur.r.b + 3) & ~3u : 0u;
-                    mt[kP + sg] = cur.sl - (copies ? cur.r.a + cur.r.b : 0u) - baseL;
+                    mt[kP + sg] = cur.sl - (copies && !srch ? cur.r.a + cur.r.b : 0u) - baseL;
+                    mt[kS + sg] = cur.ss - (srch ? cur.r.a : 0u) - baseS;
                     mt[kOffA + sg] = dst + hA;
                     mt[kLenA + sg] = copies ? cur.r.a : 0u;
                     mt[kOffB + sg] = dst + wa + hB;
@@ -389,7 +415,9 @@ __global__ void k_si_stream(SiArgs s, uint32_t *out, unsigned long long *head, S
                     mt[2] = (uint32_t)cur.base;
                     mt[3] = (uint32_t)(cur.base >> 32);
                     mt[4] = L;
+                    mt[5] = LS;
                     mt[kP + nseg] = L;
+                    mt[kS + nseg] = LS;
                     mbar_arrive_expect_tx(bar, tx);
                 }
                 __syncwarp();
@@ -457,8 +485,11 @@ __global__ void k_si_stream(SiArgs s, uint32_t *out, unsigned long long *head, S
             mt[2] = (uint32_t)pk;
             mt[3] = (uint32_t)(pk >> 32);
             mt[4] = na + nbb;
+            mt[5] = 0;
             mt[kP] = 0;
             mt[kP + 1] = na + nbb;
+            mt[kS] = 0;
+            mt[kS + 1] = 0;
             mt[kOffA] = hA;
             mt[kLenA] = na;
             mt[kOffB] = resA / 4 + hB;
@@ -521,6 +552,18 @@ __global__ void k_si_stream(SiArgs s, uint32_t *out, unsigned long long *head, S
                 ++sg;
                 while (d0 < d1 && mt[kP + sg + 1] <= d0) ++sg;  // skip empty segments
             }
+        }
+        // searched segments: lane t takes short-list elements t, t + 32, ... of all of them
+        // and finds each in its long list (both lists in the slot, long one sentinel-ended)
+        const uint32_t LS = mt[5];
+        for (uint32_t t = (uint32_t)lane; t < LS; t += 32) {
+            uint32_t sg = 0;  // last segment whose first searched element is at or before t
+#pragma unroll
+            for (uint32_t st = kMaxSeg / 2; st; st >>= 1)
+                if (sg + st < nseg && mt[kS + sg + st] <= t) sg += st;
+            const uint32_t x = slot[mt[kOffA + sg] + (t - mt[kS + sg])];
+            const uint32_t *B = slot + mt[kOffB + sg];
+            if (B[smem_lower_bound(B, mt[kLenB + sg], x)] == x) atomicAdd(cnt + sg, 1u);
         }
         __syncwarp();
         const uint64_t obase = (uint64_t)mt[2] | ((uint64_t)mt[3] << 32);
