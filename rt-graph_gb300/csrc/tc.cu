@@ -251,52 +251,6 @@ __device__ __forceinline__ uint32_t stream_item(const uint32_t *__restrict__ adj
     return cnt;
 }
 
-// Edge-at-a-time stream for a test whose f(idle) is 0: the first 128 elements of a suffix
-// are four coalesced loads per lane issued together (most suffixes are shorter), the next
-// edge's four are issued before this edge's elements are tested, and a longer suffix
-// continues in further 128-element steps. Per-element bookkeeping is one compare; the
-// edge bookkeeping is two shuffles.
-template <class F>
-__device__ __forceinline__ uint32_t stream_edges(const uint32_t *__restrict__ adj,
-                                                 const uint2 *__restrict__ rng, uint32_t k0,
-                                                 uint32_t k1, int lane, uint32_t idle, F f) {
-    auto load4 = [&](uint32_t x0, uint32_t y, uint32_t (&w)[4]) {
-#pragma unroll
-        for (int j = 0; j < 4; ++j) {
-            const uint32_t i = x0 + (uint32_t)lane + 32u * j;
-            w[j] = i < y ? __ldg(adj + i) : idle;
-        }
-    };
-    uint32_t cnt = 0;
-    uint2 nx = (k0 + lane < k1) ? __ldg(rng + k0 + lane) : make_uint2(0u, 0u);
-    for (uint32_t kb = k0; kb < k1; kb += 32) {
-        const uint32_t nb = min(32u, k1 - kb);
-        const uint2 my = nx;
-        nx = (kb + 32 + lane < k1) ? __ldg(rng + kb + 32 + lane) : make_uint2(0u, 0u);
-        uint32_t X = __shfl_sync(kFull, my.x, 0), Y = __shfl_sync(kFull, my.y, 0);
-        uint32_t w[4];
-        load4(X, Y, w);
-        for (uint32_t e = 0; e < nb; ++e) {
-            const bool more = e + 1 < nb;
-            const uint32_t Xn = __shfl_sync(kFull, my.x, more ? e + 1 : e);
-            const uint32_t Yn = more ? __shfl_sync(kFull, my.y, e + 1) : Xn;
-            uint32_t wn[4];
-            load4(Xn, Yn, wn);
-            cnt += f(w[0]) + f(w[1]) + f(w[2]) + f(w[3]);
-            for (uint32_t x0 = X + 128; x0 < Y; x0 += 128) {
-                uint32_t t[4];
-                load4(x0, Y, t);
-                cnt += f(t[0]) + f(t[1]) + f(t[2]) + f(t[3]);
-            }
-            X = Xn;
-            Y = Yn;
-#pragma unroll
-            for (int j = 0; j < 4; ++j) w[j] = wn[j];
-        }
-    }
-    return cnt;
-}
-
 // acc[0] = total, acc[1] = item queue head, acc[2] = number of items
 __global__ void k_tc_warp(const uint64_t *__restrict__ off, const uint32_t *__restrict__ adj,
                           const uint64_t *__restrict__ in_off, const uint2 *__restrict__ in_rng,
@@ -348,11 +302,11 @@ __global__ void k_tc_warp(const uint64_t *__restrict__ off, const uint32_t *__re
         __syncwarp();
         if (mode == 0) {
             const uint32_t base = v + 1;
-            cnt += stream_edges(adj, in_rng + kin, k0, k1, lane, base + 32 * p.R,
-                                [&](uint32_t w) -> uint32_t {
-                                    const uint32_t o = w - base;
-                                    return __funnelshift_r(reg[o >> 5], 0u, o) & 1u;
-                                });
+            cnt += stream_item<false>(adj, in_rng + kin, k0, k1, lane, base + 32 * p.R,
+                                      [&](uint32_t w) -> uint32_t {
+                                          const uint32_t o = w - base;
+                                          return __funnelshift_r(reg[o >> 5], 0u, o) & 1u;
+                                      });
         } else if (mode == 1) {
             cnt += stream_item<true>(adj, in_rng + kin, k0, k1, lane, kEmpty,
                                      [&](uint32_t w) -> uint32_t { return hash_probe(reg, lg, w); });
