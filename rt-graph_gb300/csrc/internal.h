@@ -146,8 +146,9 @@ rtg_status csr_build_count(rtg_ctx *ctx, const Csr &c, CountCsr &cc);
 // With in_scratch the counting form's arrays live in a context scratch slot (reused by the
 // next such build); the caller must detach them (null the pointers) before the graph dies.
 // With raw_degree vertices are ranked by their degree in the input list (duplicates and
-// self loops counted), which saves the sort that removes duplicates before ranking: a
-// different orientation of the same simple graph, so the same triangle total.
+// self loops counted; on long lists a 1-in-4 sample of it), which saves the sort that
+// removes duplicates before ranking: a different orientation of the same simple graph,
+// so the same triangle total.
 rtg_status build_count_direct(rtg_ctx *ctx, rtg_graph *g, bool in_scratch = false,
                               bool raw_degree = false);
 rtg_status graph_free_csr(Csr &c);
