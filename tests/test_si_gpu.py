@@ -99,6 +99,10 @@ def test_generated_workload_known_answers(ctx, family):
     dict(si_stage_bytes=512), dict(si_stage_bytes=512, si_stage_slots=2, si_block_warps=1),
     dict(si_stage_bytes=1024, si_stage_slots=16, si_block_warps=2),
     dict(si_stage_bytes=32768, si_stage_slots=2, si_block_warps=1), dict(si_blocks_per_sm=1),
+    # search ratio 1: nearly every pair searched (in the slot or in global memory);
+    # 1000: nearly every pair merged or chunked
+    dict(si_search_ratio=1), dict(si_search_ratio=1000),
+    dict(si_search_ratio=2, si_stage_bytes=1024, si_stage_slots=3),
 ])
 def test_batched_schedules_agree(ctx, cfg):
     """Small staging slots cut most pairs into many chunk pairs; results must not change."""
