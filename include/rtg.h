@@ -382,6 +382,8 @@ typedef struct rtg_serve_stats {
 rtg_status rtg_serve_start(int device, const rtg_serve_config *cfg, rtg_server **out);
 /* Cancels queued requests, waits for launches in flight, frees every graph. */
 void rtg_serve_stop(rtg_server *s);
+/* Text of the server's most recent error; the returned string belongs to the calling
+ * thread and stays valid until that thread's next call. */
 const char *rtg_serve_last_error(const rtg_server *s);
 /* Build a resident graph from host edges (copied). RTG_ERR_OOM when it does not fit the
  * budget, RTG_ERR_BUSY when every graph slot is taken. */

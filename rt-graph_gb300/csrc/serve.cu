@@ -690,7 +690,13 @@ void rtg_serve_stop(rtg_server *s) {
 
 const char *rtg_serve_last_error(const rtg_server *s) {
     if (!s) return "null server";
-    return s->last_error.c_str();
+    // the engine thread may record a new error at any time: hand out a copy owned by the
+    // calling thread (valid until its next call)
+    thread_local std::string copy;
+    rtg_server *m = const_cast<rtg_server *>(s);
+    std::lock_guard<std::mutex> lk(m->err_mu);
+    copy = m->last_error;
+    return copy.c_str();
 }
 
 rtg_status rtg_serve_add_graph(rtg_server *s, const uint32_t *src, const uint32_t *dst,
