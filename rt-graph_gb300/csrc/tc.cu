@@ -251,6 +251,50 @@ __device__ __forceinline__ uint32_t stream_item(const uint32_t *__restrict__ adj
     return cnt;
 }
 
+// The same item as one flat sequence, for short suffixes: the suffix lengths of 32 in-edges
+// are scanned across the lanes, and each 32-position window of their concatenation is
+// spread over the lanes (a lane finds the in-edge holding its position with five shuffle
+// steps of a binary search over the scanned starts), so a block is full even when every
+// suffix holds a few elements. Four windows' loads are in flight together.
+template <class F>
+__device__ __forceinline__ uint32_t stream_item_flat(const uint32_t *__restrict__ adj,
+                                                     const uint2 *__restrict__ rng, uint32_t k0,
+                                                     uint32_t k1, int lane, F f) {
+    uint32_t cnt = 0;
+    uint2 nx = (k0 + lane < k1) ? __ldg(rng + k0 + lane) : make_uint2(0u, 0u);
+    for (uint32_t kb = k0; kb < k1; kb += 32) {
+        const uint2 my = nx;
+        nx = (kb + 32 + lane < k1) ? __ldg(rng + kb + 32 + lane) : make_uint2(0u, 0u);
+        const uint32_t len = my.y - my.x;  // lanes past the item hold (0, 0)
+        uint32_t inc = len;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t t = __shfl_up_sync(kFull, inc, o);
+            if (lane >= o) inc += t;
+        }
+        const uint32_t T = __shfl_sync(kFull, inc, 31);
+        const uint32_t ex = inc - len;  // first position of this lane's suffix
+        for (uint32_t t0 = 0; t0 < T; t0 += 128) {
+            uint32_t w[4];
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                const uint32_t pos = t0 + 32u * j + (uint32_t)lane;
+                uint32_t e = 0;  // last in-edge whose suffix starts at or before pos
+#pragma unroll
+                for (uint32_t st = 16; st; st >>= 1)
+                    if (__shfl_sync(kFull, ex, e + st) <= pos) e += st;
+                const uint32_t xe = __shfl_sync(kFull, my.x, e);
+                const uint32_t se = __shfl_sync(kFull, ex, e);
+                w[j] = pos < T ? __ldg(adj + xe + (pos - se)) : kEmpty;
+            }
+#pragma unroll
+            for (int j = 0; j < 4; ++j)
+                if (t0 + 32u * j + (uint32_t)lane < T) cnt += f(w[j]);
+        }
+    }
+    return cnt;
+}
+
 // acc[0] = total, acc[1] = item queue head, acc[2] = number of items
 __global__ void k_tc_warp(const uint64_t *__restrict__ off, const uint32_t *__restrict__ adj,
                           const uint64_t *__restrict__ in_off, const uint2 *__restrict__ in_rng,
@@ -308,8 +352,9 @@ __global__ void k_tc_warp(const uint64_t *__restrict__ off, const uint32_t *__re
                                           return __funnelshift_r(reg[o >> 5], 0u, o) & 1u;
                                       });
         } else if (mode == 1) {
-            cnt += stream_item<true>(adj, in_rng + kin, k0, k1, lane, kEmpty,
-                                     [&](uint32_t w) -> uint32_t { return hash_probe(reg, lg, w); });
+            // low-rank vertices: short out-lists and short suffixes, streamed flat
+            cnt += stream_item_flat(adj, in_rng + kin, k0, k1, lane,
+                                    [&](uint32_t w) -> uint32_t { return hash_probe(reg, lg, w); });
         } else {
             for (uint32_t kk = k0; kk < k1; ++kk) {
                 const uint2 r = __ldg(in_rng + kin + kk);
