@@ -332,15 +332,15 @@ __global__ void k_tc_warp(const uint64_t *__restrict__ off, const uint32_t *__re
                 atomicOr(&reg[o >> 5], 1u << (o & 31));
             }
         } else if (mode == 1) {
-            lg = 5;
-            while ((1u << lg) < 2 * b) ++lg;  // 2b <= R keeps (1 << lg) <= R for R a power of 2
-            for (uint32_t q = lane; q < (1u << lg); q += 32) reg[q] = kEmpty;
-            __syncwarp();
-            const uint32_t mask = (1u << lg) - 1;
+            // open addressing over the whole region (R slots, load b/R <= 1/2, mostly far
+            // less, so probes rarely go past the first slot); 0 marks an empty slot: every
+            // element of N+(v) is a rank above v, never 0, and the region is all-zero
+            lg = 31 - __clz(p.R);
+            const uint32_t mask = p.R - 1;
             for (uint32_t q = lane; q < b; q += 32) {
                 const uint32_t w = __ldg(Nv + q);
                 uint32_t sl = hash_slot(w, lg);
-                while (atomicCAS(&reg[sl], kEmpty, w) != kEmpty) sl = (sl + 1) & mask;
+                while (atomicCAS(&reg[sl], 0u, w) != 0u) sl = (sl + 1) & mask;
             }
         }
         __syncwarp();
@@ -353,8 +353,16 @@ __global__ void k_tc_warp(const uint64_t *__restrict__ off, const uint32_t *__re
                                       });
         } else if (mode == 1) {
             // low-rank vertices: short out-lists and short suffixes, streamed flat
-            cnt += stream_item_flat(adj, in_rng + kin, k0, k1, lane,
-                                    [&](uint32_t w) -> uint32_t { return hash_probe(reg, lg, w); });
+            const uint32_t mask = p.R - 1;
+            cnt += stream_item_flat(adj, in_rng + kin, k0, k1, lane, [&](uint32_t w) -> uint32_t {
+                uint32_t sl = hash_slot(w, lg);
+                while (true) {
+                    const uint32_t x = reg[sl];
+                    if (x == w) return 1u;
+                    if (x == 0u) return 0u;
+                    sl = (sl + 1) & mask;
+                }
+            });
         } else {
             for (uint32_t kk = k0; kk < k1; ++kk) {
                 const uint2 r = __ldg(in_rng + kin + kk);
@@ -366,7 +374,15 @@ __global__ void k_tc_warp(const uint64_t *__restrict__ off, const uint32_t *__re
         if (mode == 0) {
             for (uint32_t q = lane; q < b; q += 32) reg[(__ldg(Nv + q) - v - 1) >> 5] = 0u;
         } else if (mode == 1) {
-            for (uint32_t q = lane; q < (1u << lg); q += 32) reg[q] = 0u;
+            // zero the b occupied slots (each lane finds its elements again; a slot zeroed
+            // by another lane never ends a search, which stops only on its own element)
+            const uint32_t mask = p.R - 1;
+            for (uint32_t q = lane; q < b; q += 32) {
+                const uint32_t w = __ldg(Nv + q);
+                uint32_t sl = hash_slot(w, lg);
+                while (reg[sl] != w) sl = (sl + 1) & mask;
+                reg[sl] = 0u;
+            }
         }
         __syncwarp();
     }
