@@ -13,11 +13,11 @@
 //           suffix of N+(u) after v can meet N+(v), so each in-edge is a ready-made element
 //           range. A work item is (v, first in-edge): up to E in-edges of one vertex v, taken
 //           by one warp from a device queue (persistent kernel, no block barriers). The warp
-//           marks N+(v) in its shared-memory region: as a bitmap over the ranks (v, n) when
-//           n - v - 1 fits the region (high-rank v, which carry almost all of the work on
-//           power-law graphs), else as an open-addressing hash table, else (out-list too long
-//           for the table) it falls back to a tile merge. It then streams the suffixes of the
-//           item's in-edges as 32-element blocks (one coalesced load per lane), eight blocks
+//           marks N+(v) in its shared-memory region: as a bitmap over the ranks [b0, n), b0 =
+//           v + 1 rounded down to a multiple of 32, when n - b0 fits the region (high-rank v,
+//           which carry almost all of the work on power-law graphs), else as an open-addressing
+//           hash table, else (out-list too long for the table) it falls back to a tile merge. It then streams the suffixes of the
+//           item's in-edges as 32-element blocks (one coalesced load per lane), six blocks
 //           in flight ahead of the one being tested, and tests every element with one
 //           shared-memory load.
 //           Streamed elements: sum over u of d+(u)(d+(u)-1)/2, about a quarter of the
@@ -193,7 +193,7 @@ struct WarpCfg {
 // are loaded one batch ahead. Lanes past the end of a suffix get `idle`; with kSkipIdle
 // they are not tested, otherwise f(idle) must be 0. f(w) tests one element. The per-lane
 // count of one item fits 32 bits (at most E in-edges of at most n elements each / 32).
-constexpr int kDepth = 8;
+constexpr int kDepth = 6;
 
 template <bool kSkipIdle, class F>
 __device__ __forceinline__ uint32_t stream_item(const uint32_t *__restrict__ adj,
@@ -207,7 +207,8 @@ __device__ __forceinline__ uint32_t stream_item(const uint32_t *__restrict__ adj
     uint32_t e = 0;
     uint32_t X = __shfl_sync(kFull, my.x, 0), Y = __shfl_sync(kFull, my.y, 0);
     bool live = true;
-    // move (e, X, Y) to the next edge with elements left; warp-uniform
+    // move (e, X, Y) to the next edge with elements left; warp-uniform. When the item is
+    // exhausted it stops with X >= Y, so every later block is all idle without a check.
     auto settle = [&]() {
         while (live && X >= Y) {
             if (++e >= nb) {
@@ -226,7 +227,6 @@ __device__ __forceinline__ uint32_t stream_item(const uint32_t *__restrict__ adj
         }
     };
     auto next_block = [&]() -> uint32_t {
-        if (!live) return idle;
         const uint32_t i = X + lane;
         const uint32_t w = i < Y ? __ldg(adj + i) : idle;
         X += 32;
@@ -323,12 +323,12 @@ __global__ void k_tc_warp(const uint64_t *__restrict__ off, const uint32_t *__re
         const uint64_t kin = in_off[v];
         const uint32_t k1 = min(k0 + p.E, (uint32_t)(in_off[v + 1] - kin));
         const uint32_t *Nv = adj + ov;
-        const uint32_t window = p.n - 1 - v;  // every element of these lists lies in (v, n)
-        const int mode = (window <= RB) ? 0 : (2 * b <= p.R ? 1 : 2);  // bitmap / hash / merge
+        const uint32_t base0 = (v + 1) & ~31u;  // bitmap origin, a multiple of 32
+        const int mode = (p.n - base0 <= RB) ? 0 : (2 * b <= p.R ? 1 : 2);  // bitmap / hash / merge
         uint32_t lg = 0;
         if (mode == 0) {
             for (uint32_t q = lane; q < b; q += 32) {
-                const uint32_t o = __ldg(Nv + q) - v - 1;
+                const uint32_t o = __ldg(Nv + q) - base0;
                 atomicOr(&reg[o >> 5], 1u << (o & 31));
             }
         } else if (mode == 1) {
@@ -345,11 +345,12 @@ __global__ void k_tc_warp(const uint64_t *__restrict__ off, const uint32_t *__re
         }
         __syncwarp();
         if (mode == 0) {
-            const uint32_t base = v + 1;
-            cnt += stream_item<false>(adj, in_rng + kin, k0, k1, lane, base + 32 * p.R,
+            // bit w - base0 of the bitmap: word (w >> 5) - (base0 >> 5), bit w & 31 (base0 is
+            // a multiple of 32); idle lanes read the guard word reg[R]
+            const uint32_t *regp = reg - (base0 >> 5);
+            cnt += stream_item<false>(adj, in_rng + kin, k0, k1, lane, base0 + 32 * p.R,
                                       [&](uint32_t w) -> uint32_t {
-                                          const uint32_t o = w - base;
-                                          return __funnelshift_r(reg[o >> 5], 0u, o) & 1u;
+                                          return __funnelshift_r(regp[w >> 5], 0u, w) & 1u;
                                       });
         } else if (mode == 1) {
             // low-rank vertices: short out-lists and short suffixes, streamed flat
@@ -372,7 +373,7 @@ __global__ void k_tc_warp(const uint64_t *__restrict__ off, const uint32_t *__re
         __syncwarp();
         // return the region to all-zero
         if (mode == 0) {
-            for (uint32_t q = lane; q < b; q += 32) reg[(__ldg(Nv + q) - v - 1) >> 5] = 0u;
+            for (uint32_t q = lane; q < b; q += 32) reg[(__ldg(Nv + q) - base0) >> 5] = 0u;
         } else if (mode == 1) {
             // zero the b occupied slots (each lane finds its elements again; a slot zeroed
             // by another lane never ends a search, which stops only on its own element)
