@@ -253,9 +253,12 @@ __device__ __forceinline__ uint32_t stream_item(const uint32_t *__restrict__ adj
 
 // The same item as one flat sequence, for short suffixes: the suffix lengths of 32 in-edges
 // are scanned across the lanes, and each 32-position window of their concatenation is
-// spread over the lanes (a lane finds the in-edge holding its position with five shuffle
-// steps of a binary search over the scanned starts), so a block is full even when every
-// suffix holds a few elements. Four windows' loads are in flight together.
+// spread over the lanes, so a block is full even when every suffix holds a few elements.
+// Each lane keeps a cursor on the in-edge holding its position (positions only grow, so the
+// cursor only moves forward, one shuffle pair per step, all lanes stepping together while
+// any lane needs to). kFlatWin windows' loads are in flight together.
+constexpr int kFlatWin = 4;
+
 template <class F>
 __device__ __forceinline__ uint32_t stream_item_flat(const uint32_t *__restrict__ adj,
                                                      const uint2 *__restrict__ rng, uint32_t k0,
@@ -273,22 +276,32 @@ __device__ __forceinline__ uint32_t stream_item_flat(const uint32_t *__restrict_
             if (lane >= o) inc += t;
         }
         const uint32_t T = __shfl_sync(kFull, inc, 31);
-        const uint32_t ex = inc - len;  // first position of this lane's suffix
-        for (uint32_t t0 = 0; t0 < T; t0 += 128) {
-            uint32_t w[4];
+        const uint32_t ex = inc - len;    // first position of this lane's suffix
+        const uint32_t dx = my.x - ex;    // adj index of position p of this suffix: p + dx
+        const uint32_t nxs = __shfl_down_sync(kFull, ex, 1);
+        const uint32_t nstart = lane == 31 ? kEmpty : nxs;  // start of the next suffix
+        // per-lane cursor: the in-edge holding this lane's position (positions only grow)
+        uint32_t e = 0, d = __shfl_sync(kFull, dx, 0), ns = __shfl_sync(kFull, nstart, 0);
+        for (uint32_t t0 = 0; t0 < T; t0 += 32 * kFlatWin) {
+            uint32_t w[kFlatWin];
 #pragma unroll
-            for (int j = 0; j < 4; ++j) {
+            for (int j = 0; j < kFlatWin; ++j) {
                 const uint32_t pos = t0 + 32u * j + (uint32_t)lane;
-                uint32_t e = 0;  // last in-edge whose suffix starts at or before pos
-#pragma unroll
-                for (uint32_t st = 16; st; st >>= 1)
-                    if (__shfl_sync(kFull, ex, e + st) <= pos) e += st;
-                const uint32_t xe = __shfl_sync(kFull, my.x, e);
-                const uint32_t se = __shfl_sync(kFull, ex, e);
-                w[j] = pos < T ? __ldg(adj + xe + (pos - se)) : kEmpty;
+                while (__any_sync(kFull, pos >= ns && pos < T)) {
+                    const bool adv = pos >= ns && pos < T;
+                    const uint32_t e2 = e + 1;
+                    const uint32_t d2 = __shfl_sync(kFull, dx, e2 & 31);
+                    const uint32_t n2 = __shfl_sync(kFull, nstart, e2 & 31);
+                    if (adv) {
+                        e = e2;
+                        d = d2;
+                        ns = n2;
+                    }
+                }
+                w[j] = pos < T ? __ldg(adj + pos + d) : kEmpty;
             }
 #pragma unroll
-            for (int j = 0; j < 4; ++j)
+            for (int j = 0; j < kFlatWin; ++j)
                 if (t0 + 32u * j + (uint32_t)lane < T) cnt += f(w[j]);
         }
     }
