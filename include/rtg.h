@@ -228,6 +228,16 @@ rtg_status rtg_tc_count(rtg_ctx *ctx, rtg_graph *g, rtg_tc_mode mode, uint64_t *
 rtg_status rtg_tc_count_host_edges(rtg_ctx *ctx, const uint32_t *src, const uint32_t *dst,
                                    uint64_t m, rtg_orient orient, rtg_tc_mode mode,
                                    uint64_t *out_total, rtg_timing *timing);
+/* Per-edge triangle lists on the oriented CSR of g (built with rtg_csr_build, or a host
+ * CSR): for oriented edge e = (u -> v) in CSR order (u its row, v = adj[e]) the ids w of
+ * N+(u) ∩ N+(v), ascending, in out_elems[out_offsets[e] .. out_offsets[e+1]). Every
+ * triangle of the graph appears exactly once, as (u, v, w) for its edge e = (u -> v);
+ * out_offsets[m] is the triangle count. The reference only counts (tc/bs_tc/bs_tc.cu:
+ * 120-148); the lists are the same sum written out. out_offsets has m + 1 entries; when
+ * out_capacity is too small the call fails with RTG_ERR_INVALID_ARG and out_offsets[m]
+ * holds the number of entries needed. Host arrays. */
+rtg_status rtg_tc_list(rtg_ctx *ctx, rtg_graph *g, uint64_t *out_offsets, uint32_t *out_elems,
+                       uint64_t out_capacity, rtg_timing *timing);
 /* Replaces CountOnGPU (tc/bs_tc/bs_tc.h:5): host int32 CSR in, count out (uint64
  * instead of the reference's uint32). */
 rtg_status rtg_tc_count_host_csr(rtg_ctx *ctx, const int32_t *offsets, const int32_t *adjs,

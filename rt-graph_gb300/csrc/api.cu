@@ -870,31 +870,13 @@ rtg_status rtg_si_count_dense(rtg_ctx *ctx, const rtg_sets *s, uint32_t a_begin,
     return si_run(ctx, ps, nullptr, nullptr, out_counts, flags & ~RTG_PAIRS_DEVICE, timing);
 }
 
-rtg_status rtg_si_materialize(rtg_ctx *ctx, const rtg_sets *s, const uint32_t *pair_a,
-                              const uint32_t *pair_b, uint64_t npairs, uint64_t *out_offsets,
-                              uint32_t *out_elems, uint64_t out_capacity, rtg_timing *timing) {
-    if (!ctx || !s || !out_offsets || (npairs && (!pair_a || !pair_b))) return RTG_ERR_INVALID_ARG;
-    if (npairs > 0xFFFFFFFFull)
-        return fail(ctx, RTG_ERR_INVALID_ARG, "at most 2^32-1 pairs per call");
-    double t0 = now_ms();
-    uint64_t l0 = ctx->launches;
+// Count -> scan -> write for the pairs of ps, then the offsets and elements to the host.
+static rtg_status materialize_to_host(rtg_ctx *ctx, const PairSpec &ps, uint64_t *out_offsets,
+                                      uint32_t *out_elems, uint64_t out_capacity,
+                                      rtg_timing *timing, double t0, uint64_t l0) {
+    const uint64_t npairs = ps.npairs;
     rtg_timing tm{};
     void *p = nullptr;
-    RTG_TRY(scratch(ctx, 3, npairs * 8 + 16, &p));
-    uint32_t *d_pa = (uint32_t *)p, *d_pb = d_pa + npairs;
-    if (npairs) {
-        RTG_CUDA(ctx, cudaMemcpyAsync(d_pa, pair_a, npairs * 4, cudaMemcpyHostToDevice,
-                                      ctx->stream));
-        RTG_CUDA(ctx, cudaMemcpyAsync(d_pb, pair_b, npairs * 4, cudaMemcpyHostToDevice,
-                                      ctx->stream));
-    }
-    PairSpec ps;
-    ps.off = s->off;
-    ps.elems = s->elems;
-    ps.nsets = s->nsets;
-    ps.npairs = npairs;
-    ps.pa = d_pa;
-    ps.pb = d_pb;
     uint64_t *d_off = nullptr;
     RTG_TRY(scratch(ctx, 4, (npairs + 1) * 8, &p));
     d_off = (uint64_t *)p;
@@ -915,16 +897,83 @@ rtg_status rtg_si_materialize(rtg_ctx *ctx, const rtg_sets *s, const uint32_t *p
         RTG_CUDA(ctx, cudaMemcpyAsync(out_elems, d_elems, needed * 4, cudaMemcpyDeviceToHost,
                                       ctx->stream));
     RTG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    RTG_TRY(check_status_word(ctx));
     if (st != RTG_OK)
         return fail(ctx, RTG_ERR_INVALID_ARG, "output capacity %llu < %llu elements needed",
                     (unsigned long long)out_capacity, (unsigned long long)needed);
     float ms = 0;
     cudaEventElapsedTime(&ms, ctx->ev[0], ctx->ev[1]);
     tm.count_ms = ms;
+    tm.d2h_bytes = (npairs + 1) * 8 + needed * 4;
     tm.kernel_launches = ctx->launches - l0;
     tm.total_ms = now_ms() - t0;
     if (timing) *timing = tm;
     return RTG_OK;
+}
+
+rtg_status rtg_si_materialize(rtg_ctx *ctx, const rtg_sets *s, const uint32_t *pair_a,
+                              const uint32_t *pair_b, uint64_t npairs, uint64_t *out_offsets,
+                              uint32_t *out_elems, uint64_t out_capacity, rtg_timing *timing) {
+    if (!ctx || !s || !out_offsets || (npairs && (!pair_a || !pair_b))) return RTG_ERR_INVALID_ARG;
+    if (npairs > 0xFFFFFFFFull)
+        return fail(ctx, RTG_ERR_INVALID_ARG, "at most 2^32-1 pairs per call");
+    double t0 = now_ms();
+    uint64_t l0 = ctx->launches;
+    void *p = nullptr;
+    RTG_TRY(scratch(ctx, 3, npairs * 8 + 16, &p));
+    uint32_t *d_pa = (uint32_t *)p, *d_pb = d_pa + npairs;
+    if (npairs) {
+        RTG_CUDA(ctx, cudaMemcpyAsync(d_pa, pair_a, npairs * 4, cudaMemcpyHostToDevice,
+                                      ctx->stream));
+        RTG_CUDA(ctx, cudaMemcpyAsync(d_pb, pair_b, npairs * 4, cudaMemcpyHostToDevice,
+                                      ctx->stream));
+    }
+    PairSpec ps;
+    ps.off = s->off;
+    ps.elems = s->elems;
+    ps.nsets = s->nsets;
+    ps.npairs = npairs;
+    ps.pa = d_pa;
+    ps.pb = d_pb;
+    return materialize_to_host(ctx, ps, out_offsets, out_elems, out_capacity, timing, t0, l0);
+}
+
+__global__ void k_row_ids(const uint64_t *off, uint32_t n, uint32_t *src) {
+    for (uint64_t v = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; v < n;
+         v += (uint64_t)gridDim.x * blockDim.x)
+        for (uint64_t e = off[v]; e < off[v + 1]; ++e) src[e] = (uint32_t)v;
+}
+
+rtg_status rtg_tc_list(rtg_ctx *ctx, rtg_graph *g, uint64_t *out_offsets, uint32_t *out_elems,
+                       uint64_t out_capacity, rtg_timing *timing) {
+    if (!ctx || !g || !out_offsets || (out_capacity && !out_elems)) return RTG_ERR_INVALID_ARG;
+    const Csr &c = g->ori;
+    if (!c.built) return fail(ctx, RTG_ERR_STATE, "oriented CSR not built (rtg_csr_build)");
+    if (c.m > 0xFFFFFFFFull)
+        return fail(ctx, RTG_ERR_INVALID_ARG, "at most 2^32-1 oriented edges for listing");
+    double t0 = now_ms();
+    uint64_t l0 = ctx->launches;
+    // the pairs are the edges themselves: (row of e, adj[e]) over the CSR's own rows
+    const uint32_t *src = c.src;
+    if (!src && c.m) {
+        void *p = nullptr;
+        RTG_TRY(scratch(ctx, 3, c.m * 4, &p));
+        uint32_t *d_src = (uint32_t *)p;
+        const int grid = (int)std::max<uint64_t>(1, std::min<uint64_t>((c.n + 255) / 256,
+                                                                        ctx->sm_count * 16ull));
+        k_row_ids<<<grid, 256, 0, ctx->stream>>>(c.off, c.n, d_src);
+        ctx->launches++;
+        RTG_CUDA(ctx, cudaGetLastError());
+        src = d_src;
+    }
+    PairSpec ps;
+    ps.off = c.off;
+    ps.elems = c.adj;
+    ps.nsets = c.n;
+    ps.npairs = c.m;
+    ps.pa = src;
+    ps.pb = c.adj;
+    return materialize_to_host(ctx, ps, out_offsets, out_elems, out_capacity, timing, t0, l0);
 }
 
 rtg_status rtg_graph_pair_count(rtg_ctx *ctx, rtg_graph *g, const uint32_t *u, const uint32_t *v,

@@ -153,6 +153,7 @@ _SIGS = {
                                      C.c_uint32, C.POINTER(Timing)]),
     "rtg_si_materialize": (C.c_int, [P, P, P, P, C.c_uint64, P, P, C.c_uint64,
                                      C.POINTER(Timing)]),
+    "rtg_tc_list": (C.c_int, [P, P, P, P, C.c_uint64, C.POINTER(Timing)]),
     "rtg_tune_tc": (C.c_int, [P, P, C.c_char_p, C.POINTER(TuneResult)]),
     "rtg_tune_si": (C.c_int, [P, P, P, P, C.c_uint64, C.c_char_p, C.POINTER(TuneResult)]),
     "rtg_serve_start": (C.c_int, [C.c_int, C.POINTER(ServeConfig), C.POINTER(P)]),
@@ -490,6 +491,22 @@ class Graph:
 
     def device_bytes(self) -> int:
         return lib.rtg_graph_device_bytes(self.h)
+
+    def tc_list(self, capacity: int | None = None):
+        """Per-edge triangle lists on the oriented CSR: (offsets u64[m+1], w u32[T], timing);
+        the triangles of edge e = (u -> v) of csr() are (u, v, w[offsets[e]:offsets[e+1]])."""
+        m = self.info().m
+        off = np.empty(m + 1, np.uint64)
+        if capacity is None:
+            st = lib.rtg_tc_list(self.ctx.h, self.h, _ptr(off), None, 0, None)
+            if st not in (OK, ERR_INVALID_ARG):
+                self.ctx.check(st, "tc_list")
+            capacity = int(off[-1])
+        w = np.empty(max(capacity, 1), np.uint32)
+        t = Timing()
+        self.ctx.check(lib.rtg_tc_list(self.ctx.h, self.h, _ptr(off), _ptr(w), capacity,
+                                       C.byref(t)), "tc_list")
+        return off, w[: int(off[-1])], t
 
     def tc(self, mode: int = TC_BATCHED):
         out = C.c_uint64(0)

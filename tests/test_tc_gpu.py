@@ -142,6 +142,51 @@ def test_one_shot_host_edges_all_golden(ctx, name):
         assert got == rec["triangles"], (name, mode)
 
 
+@pytest.mark.parametrize("name", ["k4_noise", "ba_n4096_m4_s7", "rmat_s12_ef16_s1",
+                                  "rmat_s14_ef16_s42"])
+def test_triangle_lists_match_oracle(ctx, name):
+    """rtg_tc_list: per-edge lists N+(u) ∩ N+(v) over the oriented CSR, bit-exact against the
+    oracle's per-pair merge; the lists hold exactly the reference's triangle count, and
+    every listed (u, v, w) is a triangle of the simple undirected graph."""
+    rec = TC[name]
+    s, d = golden_edges(rec)
+    g = ctx.graph_from_edges(s, d).build(rtg.ORIENT_DEGREE)
+    off, adj = g.csr()
+    n = len(off) - 1
+    src = np.repeat(np.arange(n, dtype=np.uint32), np.diff(off.astype(np.int64)))
+    loff, w, t = g.tc_list()
+    assert int(loff[-1]) == rec["triangles"] and len(w) == rec["triangles"]
+    ooff, ow = oracle.si_materialize(off, adj, src, adj)
+    assert np.array_equal(loff, ooff)
+    assert np.array_equal(w, ow)
+    e = np.repeat(np.arange(len(adj)), np.diff(loff.astype(np.int64)))
+    u, v, x = src[e].astype(np.int64), adj[e].astype(np.int64), w.astype(np.int64)
+    a, b = np.minimum(s, d).astype(np.int64), np.maximum(s, d).astype(np.int64)
+    keys = np.unique(a[a != b] * (1 << 32) + b[a != b])
+
+    def has(p, q):
+        k = np.minimum(p, q) * (1 << 32) + np.maximum(p, q)
+        return np.isin(k, keys)
+
+    assert has(u, v).all() and has(u, x).all() and has(v, x).all()
+    assert len(np.unique((np.sort(np.stack([u, v, x]), axis=0) * [[1 << 42], [1 << 21], [1]]).sum(0))) == len(w)
+
+
+def test_triangle_lists_capacity_and_state(ctx):
+    rec = TC["rmat_s12_ef16_s1"]
+    s, d = golden_edges(rec)
+    g = ctx.graph_from_edges(s, d).build(rtg.ORIENT_DEGREE)
+    m = g.info().m
+    off = np.empty(m + 1, np.uint64)
+    w = np.empty(8, np.uint32)
+    st = rtg.lib.rtg_tc_list(ctx.h, g.h, rtg._ptr(off), rtg._ptr(w), 8, None)
+    assert st == rtg.ERR_INVALID_ARG and int(off[-1]) == rec["triangles"]
+    loff, lw, _ = g.tc_list(capacity=rec["triangles"])
+    assert int(loff[-1]) == rec["triangles"]
+    raw = ctx.graph_from_edges(s, d)  # no CSR built yet
+    assert rtg.lib.rtg_tc_list(ctx.h, raw.h, rtg._ptr(off), None, 0, None) == rtg.ERR_STATE
+
+
 def test_file_formats(ctx, tmp_path):
     rec = TC["wheel"]
     s, d = golden_edges(rec)
