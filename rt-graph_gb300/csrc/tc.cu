@@ -17,8 +17,8 @@
 //           v + 1 rounded down to a multiple of 32, when n - b0 fits the region (high-rank v,
 //           which carry almost all of the work on power-law graphs), else as an open-addressing
 //           hash table, else (out-list too long for the table) it falls back to a tile merge. It then streams the suffixes of the
-//           item's in-edges as 32-element blocks (one coalesced load per lane), six blocks
-//           in flight ahead of the one being tested, and tests every element with one
+//           item's in-edges as 64-element blocks (two coalesced loads per lane), three
+//           blocks in flight ahead of the one being tested, and tests every element with one
 //           shared-memory load.
 //           Streamed elements: sum over u of d+(u)(d+(u)-1)/2, about a quarter of the
 //           push-order work on power-law graphs. Item build + count are one CUDA graph,
@@ -187,15 +187,18 @@ struct WarpCfg {
 };
 
 // Stream the suffix ranges of the item's in-edges [k0, k1) (edge k's range is in_rng[kin+k])
-// as a sequence of 32-element blocks, one coalesced 32-bit load per lane per block; a block
-// never spans two suffixes. kDepth blocks are in flight ahead of the block being tested, and
-// the pipeline runs across edge and batch boundaries; the ranges of the next 32 in-edges
-// are loaded one batch ahead. Lanes past the end of a suffix get `idle`; with kSkipIdle
-// they are not tested, otherwise f(idle) must be 0. f(w) tests one element. The per-lane
-// count of one item fits 32 bits (at most E in-edges of at most n elements each / 32).
-constexpr int kDepth = 6;
+// as a sequence of blocks of 32 * kLoads elements, kLoads coalesced 32-bit loads per lane
+// per block (elements X + lane + 32 j); a block never spans two suffixes. Two loads per
+// block halve the per-block bookkeeping against one, at 73 % full blocks instead of 86 % on
+// R-MAT-21's suffixes. kDepth blocks are in flight ahead of the block being tested, and the
+// pipeline runs across edge and batch boundaries; the ranges of the next 32 in-edges are
+// loaded one batch ahead. Elements past the end of a suffix read as `idle`, and f(idle)
+// must be 0. f(w) tests one element. The per-lane count of one item fits 32 bits (at most
+// E in-edges of at most n elements each / 32).
+constexpr int kLoads = 2;
+constexpr int kDepth = 3;
 
-template <bool kSkipIdle, class F>
+template <class F>
 __device__ __forceinline__ uint32_t stream_item(const uint32_t *__restrict__ adj,
                                                 const uint2 *__restrict__ rng, uint32_t k0,
                                                 uint32_t k1, int lane, uint32_t idle, F f) {
@@ -226,28 +229,34 @@ __device__ __forceinline__ uint32_t stream_item(const uint32_t *__restrict__ adj
             Y = __shfl_sync(kFull, my.y, e);
         }
     };
-    auto next_block = [&]() -> uint32_t {
+    struct Block {
+        uint32_t w[kLoads];
+    };
+    auto next_block = [&]() -> Block {
         const uint32_t i = X + lane;
-        const uint32_t w = i < Y ? __ldg(adj + i) : idle;
-        X += 32;
+        Block b;
+#pragma unroll
+        for (int j = 0; j < kLoads; ++j) b.w[j] = i + 32 * j < Y ? __ldg(adj + i + 32 * j) : idle;
+        X += 32 * kLoads;
         settle();
-        return w;
+        return b;
     };
     settle();
-    uint32_t buf[kDepth];
+    Block buf[kDepth];
 #pragma unroll
     for (int d = 0; d < kDepth; ++d) buf[d] = next_block();
     while (live) {
 #pragma unroll
         for (int d = 0; d < kDepth; ++d) {
-            const uint32_t w = buf[d];
-            if (!kSkipIdle || w != idle) cnt += f(w);
+#pragma unroll
+            for (int j = 0; j < kLoads; ++j) cnt += f(buf[d].w[j]);
             buf[d] = next_block();
         }
     }
 #pragma unroll
     for (int d = 0; d < kDepth; ++d)
-        if (!kSkipIdle || buf[d] != idle) cnt += f(buf[d]);
+#pragma unroll
+        for (int j = 0; j < kLoads; ++j) cnt += f(buf[d].w[j]);
     return cnt;
 }
 
@@ -361,10 +370,10 @@ __global__ void k_tc_warp(const uint64_t *__restrict__ off, const uint32_t *__re
             // bit w - base0 of the bitmap: word (w >> 5) - (base0 >> 5), bit w & 31 (base0 is
             // a multiple of 32); idle lanes read the guard word reg[R]
             const uint32_t *regp = reg - (base0 >> 5);
-            cnt += stream_item<false>(adj, in_rng + kin, k0, k1, lane, base0 + 32 * p.R,
-                                      [&](uint32_t w) -> uint32_t {
-                                          return __funnelshift_r(regp[w >> 5], 0u, w) & 1u;
-                                      });
+            cnt += stream_item(adj, in_rng + kin, k0, k1, lane, base0 + 32 * p.R,
+                               [&](uint32_t w) -> uint32_t {
+                                   return __funnelshift_r(regp[w >> 5], 0u, w) & 1u;
+                               });
         } else if (mode == 1) {
             // low-rank vertices: short out-lists and short suffixes, streamed flat
             const uint32_t mask = p.R - 1;
