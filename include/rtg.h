@@ -116,7 +116,8 @@ typedef enum rtg_tc_mode { RTG_TC_PLAIN = 0, RTG_TC_BATCHED = 1 } rtg_tc_mode;
 /* Per-call timing and counters. All times in milliseconds. Device times come from CUDA
  * events on the context stream. */
 typedef struct rtg_timing {
-    double h2d_ms;            /* host -> device copies made by the call           */
+    double h2d_ms;            /* host -> device copies made by the call (0 when the
+                                 kernel reads page-locked host memory itself)      */
     double build_ms;          /* CSR build / set upload stage                     */
     double count_ms;          /* counting stage (all kernels of the stage)        */
     double main_kernel_ms;    /* the dominant counting kernel alone               */
@@ -286,7 +287,10 @@ uint64_t rtg_sets_elems(const rtg_sets *s);
 void rtg_sets_destroy(rtg_sets *s);
 
 /* |S[pair_a[i]] ∩ S[pair_b[i]]| for i < npairs. flags: RTG_SI_* family, RTG_PAIRS_DEVICE,
- * RTG_OUT_DEVICE. */
+ * RTG_OUT_DEVICE. Host pair and count arrays in page-locked memory (rtg_host_alloc,
+ * cudaHostAlloc, cudaHostRegister) are read and written by the kernel itself over the
+ * host link, with no staging copies (timing->h2d_bytes / d2h_bytes count the bytes moved,
+ * h2d_ms / d2h_ms stay 0); pageable host arrays are copied through device memory. */
 rtg_status rtg_si_count(rtg_ctx *ctx, const rtg_sets *s, const uint32_t *pair_a,
                         const uint32_t *pair_b, uint64_t npairs, uint32_t *out_counts,
                         uint32_t flags, rtg_timing *timing);

@@ -763,6 +763,17 @@ void rtg_sets_destroy(rtg_sets *s) {
 
 /* ------------------------------------------------------ set intersection */
 
+// Device address of a page-locked host array that the GPU can address directly (pinned
+// memory is mapped into the device's address space), or nullptr for pageable memory.
+static void *mapped_host(const void *p) {
+    cudaPointerAttributes a{};
+    if (!p || cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();  // not a CUDA pointer: clear the non-sticky error
+        return nullptr;
+    }
+    return a.type == cudaMemoryTypeHost ? a.devicePointer : nullptr;
+}
+
 static rtg_status si_run(rtg_ctx *ctx, PairSpec &ps, const uint32_t *pair_a,
                          const uint32_t *pair_b, uint32_t *out, uint32_t flags, rtg_timing *t) {
     double t0 = now_ms();
@@ -773,10 +784,24 @@ static rtg_status si_run(rtg_ctx *ctx, PairSpec &ps, const uint32_t *pair_a,
     uint64_t np = ps.npairs;
     uint32_t *d_pa = nullptr, *d_pb = nullptr, *d_out = nullptr;
     rtg_timing tm{};
+    bool copied_in = false;
+    // Pinned host pair ids and counts are read and written by the kernel itself over the
+    // host link (no staging copies, no copy time outside the kernel); pageable ones are
+    // copied through device scratch.
+    void *mapped_a = nullptr, *mapped_b = nullptr, *mapped_out = nullptr;
+    if (np && !ps.dense_nb && !(flags & RTG_PAIRS_DEVICE)) {
+        mapped_a = mapped_host(pair_a);
+        mapped_b = mapped_a ? mapped_host(pair_b) : nullptr;
+    }
+    if (np && !(flags & RTG_OUT_DEVICE)) mapped_out = mapped_host(out);
     if (!ps.dense_nb) {
         if (flags & RTG_PAIRS_DEVICE) {
             d_pa = const_cast<uint32_t *>(pair_a);
             d_pb = const_cast<uint32_t *>(pair_b);
+        } else if (mapped_a && mapped_b) {
+            d_pa = static_cast<uint32_t *>(mapped_a);
+            d_pb = static_cast<uint32_t *>(mapped_b);
+            tm.h2d_bytes = np * 8;
         } else {
             void *p = nullptr;
             RTG_TRY(scratch(ctx, 3, np * 8 + 16, &p));
@@ -791,12 +816,16 @@ static rtg_status si_run(rtg_ctx *ctx, PairSpec &ps, const uint32_t *pair_a,
             }
             RTG_CUDA(ctx, cudaEventRecord(ctx->ev[5], ctx->stream));
             tm.h2d_bytes = np * 8;
+            copied_in = true;
         }
         ps.pa = d_pa;
         ps.pb = d_pb;
     }
     if (flags & RTG_OUT_DEVICE) {
         d_out = out;
+    } else if (mapped_out) {
+        d_out = static_cast<uint32_t *>(mapped_out);
+        tm.d2h_bytes = np * 4;
     } else {
         void *p = nullptr;
         RTG_TRY(scratch(ctx, 4, np * 4 + 16, &p));
@@ -806,7 +835,8 @@ static rtg_status si_run(rtg_ctx *ctx, PairSpec &ps, const uint32_t *pair_a,
     RTG_CUDA(ctx, cudaEventRecord(ctx->ev[0], ctx->stream));
     RTG_TRY(si_count_device(ctx, ps, d_out, family, &kms, &ctx->launches));
     RTG_CUDA(ctx, cudaEventRecord(ctx->ev[1], ctx->stream));
-    if (!(flags & RTG_OUT_DEVICE) && np) {
+    const bool copy_out = !(flags & RTG_OUT_DEVICE) && np && !mapped_out;
+    if (copy_out) {
         RTG_CUDA(ctx, cudaMemcpyAsync(out, d_out, np * 4, cudaMemcpyDeviceToHost, ctx->stream));
         tm.d2h_bytes = np * 4;
     }
@@ -817,11 +847,11 @@ static rtg_status si_run(rtg_ctx *ctx, PairSpec &ps, const uint32_t *pair_a,
     cudaEventElapsedTime(&ms, ctx->ev[0], ctx->ev[1]);
     tm.count_ms = ms;
     tm.main_kernel_ms = kms;
-    if (tm.h2d_bytes) {
+    if (copied_in) {
         cudaEventElapsedTime(&ms, ctx->ev[4], ctx->ev[5]);
         tm.h2d_ms = ms;
     }
-    if (tm.d2h_bytes) {
+    if (copy_out) {
         cudaEventElapsedTime(&ms, ctx->ev[1], ctx->ev[2]);
         tm.d2h_ms = ms;
     }
