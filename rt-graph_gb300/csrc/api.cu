@@ -552,6 +552,70 @@ rtg_status rtg_tc_count(rtg_ctx *ctx, rtg_graph *g, rtg_tc_mode mode, uint64_t *
     return RTG_OK;
 }
 
+// Device address of a page-locked host array that the GPU can address directly (pinned
+// memory is mapped into the device's address space), or nullptr for pageable memory.
+static void *mapped_host(const void *p) {
+    cudaPointerAttributes a{};
+    if (!p || cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();  // not a CUDA pointer: clear the non-sticky error
+        return nullptr;
+    }
+    return a.type == cudaMemoryTypeHost ? a.devicePointer : nullptr;
+}
+
+// Copies page-locked host edges into device memory, reading them over the host link in
+// 16-byte loads, and on the way finds the largest id and counts the raw degrees of the
+// sampled edges (edge i when i % stride == 0, the edges k_degree_raw samples) into deg,
+// for ids below cap; *d_over becomes 1 when a sampled id is at or above cap. The copy is
+// bound by the host link, so the two passes that would otherwise follow it are hidden.
+// Quad q holds edges 4q .. 4q+3; stride is 1 or a multiple of 4.
+__global__ void k_edge_pull(const uint4 *__restrict__ hs, const uint4 *__restrict__ hd,
+                            const uint32_t *__restrict__ hs1, const uint32_t *__restrict__ hd1,
+                            uint64_t m, uint4 *ds, uint4 *dd, uint32_t *ds1, uint32_t *dd1,
+                            uint32_t *deg, uint32_t cap, uint32_t stride, unsigned *d_max,
+                            unsigned *d_over) {
+    unsigned mx = 0, over = 0;
+    auto count = [&](uint32_t x) {
+        if (x < cap) atomicAdd(&deg[x], 1u);
+        else over = 1u;
+    };
+    const uint64_t m4 = m / 4;
+    for (uint64_t q = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; q < m4;
+         q += (uint64_t)gridDim.x * blockDim.x) {
+        const uint4 a = hs[q], b = hd[q];
+        ds[q] = a;
+        dd[q] = b;
+        mx = max(mx, max(max(max(a.x, a.y), max(a.z, a.w)), max(max(b.x, b.y), max(b.z, b.w))));
+        if (stride == 1) {
+            count(a.x); count(a.y); count(a.z); count(a.w);
+            count(b.x); count(b.y); count(b.z); count(b.w);
+        } else if ((4 * q) % stride == 0) {
+            count(a.x);
+            count(b.x);
+        }
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) {  // the last m % 4 edges
+        for (uint64_t i = 4 * m4; i < m; ++i) {
+            const uint32_t a = hs1[i], b = hd1[i];
+            ds1[i] = a;
+            dd1[i] = b;
+            mx = max(mx, max(a, b));
+            if (i % stride == 0) {
+                count(a);
+                count(b);
+            }
+        }
+    }
+    for (int o = 16; o; o >>= 1) {
+        mx = max(mx, __shfl_down_sync(0xffffffffu, mx, o));
+        over |= __shfl_down_sync(0xffffffffu, over, o);
+    }
+    if ((threadIdx.x & 31) == 0) {
+        atomicMax(d_max, mx);
+        if (over) atomicOr(d_over, 1u);
+    }
+}
+
 rtg_status rtg_tc_count_host_edges(rtg_ctx *ctx, const uint32_t *src, const uint32_t *dst,
                                    uint64_t m, rtg_orient orient, rtg_tc_mode mode,
                                    uint64_t *out_total, rtg_timing *timing) {
@@ -575,12 +639,42 @@ rtg_status rtg_tc_count_host_edges(rtg_ctx *ctx, const uint32_t *src, const uint
         tg.d_src = static_cast<uint32_t *>(pe);
         tg.d_dst = tg.d_src + mpad;
         tg.m_input = m;
-        if (m) {
+        // page-locked host edges are pulled in by one kernel that also finds the largest
+        // id and counts the sampled degrees (into the counters the previous one-shot build
+        // sized; when they are too small the build counts again); pageable ones are copied
+        EdgePrePass pre;
+        bool have_pre = false;
+        void *hsrc = m >= (1ull << 20) ? mapped_host(src) : nullptr;
+        void *hdst = hsrc ? mapped_host(dst) : nullptr;
+        if (hsrc && hdst &&
+            ((reinterpret_cast<uintptr_t>(hsrc) | reinterpret_cast<uintptr_t>(hdst)) & 15) == 0) {
+            DeviceBuffer &db = ctx->scratch[kDegreeSlot];
+            const uint32_t cap = (uint32_t)std::min<uint64_t>(db.bytes / 4, 0xFFFFFFFFull);
+            if (cap) RTG_CUDA(ctx, cudaMemsetAsync(db.ptr, 0, cap * 4ull, ctx->stream));
+            unsigned *d_w = reinterpret_cast<unsigned *>(ctx->d_scalars);
+            RTG_CUDA(ctx, cudaMemsetAsync(d_w, 0, 8, ctx->stream));
+            const uint32_t stride = m >= kDegreeSampleFrom ? kDegreeSample : 1u;
+            const int grid = (int)std::max<uint64_t>(
+                1, std::min<uint64_t>((m / 4 + 255) / 256, (uint64_t)ctx->sm_count * 8));
+            k_edge_pull<<<grid, 256, 0, ctx->stream>>>(
+                static_cast<const uint4 *>(hsrc), static_cast<const uint4 *>(hdst),
+                static_cast<const uint32_t *>(hsrc), static_cast<const uint32_t *>(hdst), m,
+                reinterpret_cast<uint4 *>(tg.d_src), reinterpret_cast<uint4 *>(tg.d_dst),
+                tg.d_src, tg.d_dst, static_cast<uint32_t *>(db.ptr), cap, stride, d_w, d_w + 1);
+            ctx->launches++;
+            RTG_CUDA(ctx, cudaGetLastError());
+            unsigned hw[2] = {0, 0};
+            RTG_CUDA(ctx, cudaMemcpyAsync(hw, d_w, 8, cudaMemcpyDeviceToHost, ctx->stream));
+            RTG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+            pre.maxid = hw[0];
+            pre.deg_valid = hw[1] == 0 && cap > 0 && (uint64_t)hw[0] < cap;
+            have_pre = true;
+        } else if (m) {
             RTG_CUDA(ctx, cudaMemcpyAsync(tg.d_src, src, m * 4, cudaMemcpyHostToDevice, ctx->stream));
             RTG_CUDA(ctx, cudaMemcpyAsync(tg.d_dst, dst, m * 4, cudaMemcpyHostToDevice, ctx->stream));
         }
         RTG_CUDA(ctx, cudaEventRecord(ctx->ev[7], ctx->stream));
-        rtg_status s = build_count_direct(ctx, g, true, true);
+        rtg_status s = build_count_direct(ctx, g, true, true, have_pre ? &pre : nullptr);
         void *scr = nullptr;
         const uint64_t need = s == RTG_OK ? tc_plan_estimate_bytes(ctx, g) : 0;
         if (s == RTG_OK) s = scratch(ctx, 6, need, &scr);
@@ -762,17 +856,6 @@ void rtg_sets_destroy(rtg_sets *s) {
 }
 
 /* ------------------------------------------------------ set intersection */
-
-// Device address of a page-locked host array that the GPU can address directly (pinned
-// memory is mapped into the device's address space), or nullptr for pageable memory.
-static void *mapped_host(const void *p) {
-    cudaPointerAttributes a{};
-    if (!p || cudaPointerGetAttributes(&a, p) != cudaSuccess) {
-        cudaGetLastError();  // not a CUDA pointer: clear the non-sticky error
-        return nullptr;
-    }
-    return a.type == cudaMemoryTypeHost ? a.devicePointer : nullptr;
-}
 
 static rtg_status si_run(rtg_ctx *ctx, PairSpec &ps, const uint32_t *pair_a,
                          const uint32_t *pair_b, uint32_t *out, uint32_t flags, rtg_timing *t) {

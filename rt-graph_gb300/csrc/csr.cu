@@ -351,13 +351,12 @@ __global__ void k_degree_raw(const uint32_t *s, const uint32_t *d, uint64_t m, u
     }
 }
 
-// Edge lists at least this long rank by a 1-in-kDegreeSample sample of the raw degrees:
-// an eighth of the atomics (whose hub contention made this pass 0.36 ms of the R-MAT-21
-// build at 1 in 4), hubs ordered the same (their counts are large), and the count is exact
-// for any total order. On R-MAT-21, 1 in 8 against 1 in 4: build 0.12 ms shorter, count
-// unchanged within 0.3 %; 1 in 16 saved 0.07 ms more but cost 0.7 % of the count.
-constexpr uint64_t kDegreeSampleFrom = 1ull << 22;
-constexpr uint32_t kDegreeSample = 8;
+// Edge lists of kDegreeSampleFrom edges or more rank by a 1-in-kDegreeSample sample of the
+// raw degrees (constants in internal.h): an eighth of the atomics (whose hub contention
+// made this pass 0.36 ms of the R-MAT-21 build at 1 in 4), hubs ordered the same (their
+// counts are large), and the count is exact for any total order. On R-MAT-21, 1 in 8
+// against 1 in 4: build 0.12 ms shorter, count unchanged within 0.3 %; 1 in 16 saved
+// 0.07 ms more but cost 0.7 % of the count.
 
 // degrees of the simple graph from its sorted canonical keys: the row length of the
 // smaller endpoint (offsets of the sorted keys, no atomics on the hub rows) ...
@@ -555,13 +554,18 @@ rtg_status csr_build_count(rtg_ctx *ctx, const Csr &c, CountCsr &cc) {
     return count_tail(ctx, cc, ek, other, (uint64_t)mu, n, B, src_r);
 }
 
-rtg_status build_count_direct(rtg_ctx *ctx, rtg_graph *g, bool in_scratch, bool raw_degree) {
+rtg_status build_count_direct(rtg_ctx *ctx, rtg_graph *g, bool in_scratch, bool raw_degree,
+                              const EdgePrePass *pre) {
     const uint64_t m = g->m_input;
     tc_plan_free(g->plan_batched);
     tc_plan_free(g->plan_plain);
     g->plan_batched = g->plan_plain = nullptr;
     uint32_t maxid = 0;
-    if (m) {
+    if (pre && raw_degree) {
+        maxid = pre->maxid;
+        if (m && maxid == kEmpty)
+            return fail(ctx, RTG_ERR_INVALID_ARG, "vertex id 0xFFFFFFFF is reserved");
+    } else if (m) {
         unsigned int *d_mx = (unsigned int *)ctx->d_scalars;
         RTG_CUDA(ctx, cudaMemsetAsync(d_mx, 0, 4, ctx->stream));
         k_max_id<<<grid_for(ctx, m), kThreads, 0, ctx->stream>>>(g->d_src, g->d_dst, m, d_mx);
@@ -582,17 +586,26 @@ rtg_status build_count_direct(rtg_ctx *ctx, rtg_graph *g, bool in_scratch, bool 
     if (raw_degree && m) {
         // ranks by degree in the input list (duplicates and self loops counted); the one
         // sort of the rank edge keys then also brings duplicates together for Unique
-        RTG_TRY(buf.alloc(&deg, n));
         RTG_TRY(buf.alloc(&rank, n));
         RTG_TRY(buf.alloc(&r0, n + 1ull));
         RTG_TRY(buf.alloc(&r1, n + 1ull));
         RTG_TRY(buf.alloc(&src_r, m));
-        RTG_CUDA(ctx, cudaMemsetAsync(deg, 0, n * 4ull, ctx->stream));
         const uint32_t stride = m >= kDegreeSampleFrom ? kDegreeSample : 1u;
-        k_degree_raw<<<grid_for(ctx, m / stride), kThreads, 0, ctx->stream>>>(g->d_src, g->d_dst,
-                                                                             m, stride, deg);
+        if (pre && pre->deg_valid) {
+            void *p = nullptr;
+            RTG_TRY(scratch(ctx, kDegreeSlot, n * 4ull, &p));  // counted by the pre-pass
+            deg = static_cast<uint32_t *>(p);
+        } else {
+            void *p = nullptr;
+            RTG_TRY(scratch(ctx, kDegreeSlot, n * 4ull, &p));
+            deg = static_cast<uint32_t *>(p);
+            RTG_CUDA(ctx, cudaMemsetAsync(deg, 0, n * 4ull, ctx->stream));
+            k_degree_raw<<<grid_for(ctx, m / stride), kThreads, 0, ctx->stream>>>(
+                g->d_src, g->d_dst, m, stride, deg);
+            ctx->launches++;
+        }
         k_rank_keys<<<grid_for(ctx, n), kThreads, 0, ctx->stream>>>(deg, n, B, r0);
-        ctx->launches += 2;
+        ctx->launches++;
         RTG_CUDA(ctx, cudaGetLastError());
         cub::DoubleBuffer<uint64_t> dr(r0, r1);
         RTG_TRY(radix_sort(ctx, dr, n, std::min(64, B + 32)));

@@ -77,7 +77,7 @@ struct rtg_ctx {
     unsigned long long *d_scalars = nullptr;  // small device scratch for counters (16 words)
     cudaEvent_t ev[8] = {};
     // grow-only scratch for CUB temp storage and per-call buffers
-    rtg::DeviceBuffer scratch[8];
+    rtg::DeviceBuffer scratch[9];
     // grow-only temporaries of the CSR builder (kept between builds: no allocation, and
     // none of the implicit synchronisation of a free, on repeated builds)
     rtg::DeviceBuffer work[12];
@@ -146,11 +146,21 @@ rtg_status csr_build_count(rtg_ctx *ctx, const Csr &c, CountCsr &cc);
 // With in_scratch the counting form's arrays live in a context scratch slot (reused by the
 // next such build); the caller must detach them (null the pointers) before the graph dies.
 // With raw_degree vertices are ranked by their degree in the input list (duplicates and
-// self loops counted; on long lists a 1-in-4 sample of it), which saves the sort that
-// removes duplicates before ranking: a different orientation of the same simple graph,
-// so the same triangle total.
+// self loops counted; on long lists a 1-in-kDegreeSample sample of it), which saves the
+// sort that removes duplicates before ranking: a different orientation of the same simple
+// graph, so the same triangle total.
+// pre (raw_degree only): the largest vertex id, and with deg_valid the (sampled) raw
+// degrees of ids 0..maxid already counted into scratch slot kDegreeSlot, as the pass that
+// copies pinned host edges in computes them (edge_pull in api.cu).
+struct EdgePrePass {
+    uint32_t maxid = 0;
+    bool deg_valid = false;
+};
+constexpr int kDegreeSlot = 8;               // scratch slot of the raw-degree counters
+constexpr uint64_t kDegreeSampleFrom = 1ull << 22;
+constexpr uint32_t kDegreeSample = 8;
 rtg_status build_count_direct(rtg_ctx *ctx, rtg_graph *g, bool in_scratch = false,
-                              bool raw_degree = false);
+                              bool raw_degree = false, const EdgePrePass *pre = nullptr);
 rtg_status graph_free_csr(Csr &c);
 void count_csr_free(CountCsr &cc);
 

@@ -187,6 +187,26 @@ def test_triangle_lists_capacity_and_state(ctx):
     assert rtg.lib.rtg_tc_list(ctx.h, raw.h, rtg._ptr(off), None, 0, None) == rtg.ERR_STATE
 
 
+def test_one_shot_pinned_edges_pulled(ctx):
+    """Page-locked host edges: one kernel pulls them over the host link and counts the
+    ranking degrees on the way (exact below 2^22 edges, sampled above). First call (no
+    degree counters yet), repeat (counters reused), a larger graph after a smaller one
+    (counters too small: counted again), and an edge count that is not a multiple of 4."""
+    for scale, trim in ((17, 0), (20, 0), (18, 3), (20, 1)):
+        s, d = rtg.gen_rmat(scale, 16, 0.57, 0.19, 0.19, seed=3)
+        if trim:
+            s, d = s[:-trim], d[:-trim]
+        want, _ = ctx.graph_from_edges(s, d).build(rtg.ORIENT_DEGREE).tc(rtg.TC_PLAIN)
+        hs = ctx.host_array(len(s), np.uint32)
+        hd = ctx.host_array(len(d), np.uint32)
+        hs[:] = s
+        hd[:] = d
+        for _ in range(2):
+            got, t = ctx.tc_count_host_edges(hs, hd, rtg.ORIENT_DEGREE, rtg.TC_BATCHED)
+            assert got == want, (scale, trim)
+            assert t.h2d_bytes == 8 * len(s)
+
+
 def test_file_formats(ctx, tmp_path):
     rec = TC["wheel"]
     s, d = golden_edges(rec)
