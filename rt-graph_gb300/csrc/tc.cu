@@ -173,9 +173,11 @@ __global__ void k_item_fill(const uint64_t *__restrict__ off, const uint64_t *__
         uint32_t b = (uint32_t)(off[v + 1] - off[v]);
         uint32_t indeg = (uint32_t)(in_off[v + 1] - in_off[v]);
         if (b < 1 || indeg < 1) continue;
-        uint32_t b0 = base[v];
+        // descending rank order: the many light items of low-rank vertices come last and
+        // fill in behind the heavier ones (1.4 % shorter than ascending order on R-MAT-21)
+        const uint32_t last = base[n] - 1 - base[v];
         uint32_t k = 0;
-        for (uint32_t j = 0; j < indeg; j += E, ++k) items[b0 + k] = (v << 32) | j;
+        for (uint32_t j = 0; j < indeg; j += E, ++k) items[last - k] = (v << 32) | j;
     }
     if (blockIdx.x == 0 && threadIdx.x == 0) acc[2] = base[n];
 }
@@ -338,9 +340,7 @@ __global__ void k_tc_warp(const uint64_t *__restrict__ off, const uint32_t *__re
         if (lane == 0) k = atomicAdd(&acc[1], 1ull);
         k = __shfl_sync(kFull, k, 0);
         if (k >= nitems) break;
-        // items in descending rank order: the late, light items of low-rank vertices fill
-        // in behind the heavier ones (1.4 % shorter than ascending order on R-MAT-21)
-        const uint64_t it = items[nitems - 1 - k];
+        const uint64_t it = items[k];
         const uint32_t v = (uint32_t)(it >> 32), k0 = (uint32_t)it;
         const uint64_t ov = off[v];
         const uint32_t b = (uint32_t)(off[v + 1] - ov);
@@ -503,16 +503,23 @@ rtg_status batched_shape(rtg_ctx *ctx, const CountCsr &c, const rtg_config &cfg,
     return RTG_OK;
 }
 
-// reset -> item counts -> scan -> item fill -> [k0] persistent count [k1]
-void enqueue_batched(cudaStream_t st, const CountCsr &c, const BatchedShape &bs, uint64_t *items,
-                     uint32_t *vcnt, void *cub_tmp, unsigned long long *acc, cudaEvent_t k0,
-                     cudaEvent_t k1, bool external_events) {
+// reset -> item counts -> scan -> item fill (acc[2] = number of items)
+void enqueue_items(cudaStream_t st, const CountCsr &c, const BatchedShape &bs, uint64_t *items,
+                   uint32_t *vcnt, void *cub_tmp, unsigned long long *acc) {
     uint32_t *vbase = vcnt + (c.n + 1ull);
     size_t cub_bytes = bs.cub_bytes;
     cudaMemsetAsync(acc, 0, 8 * sizeof(unsigned long long), st);
     k_item_counts<<<bs.g1, 256, 0, st>>>(c.off, c.in_off, c.n, bs.pc.E, vcnt);
     cub::DeviceScan::ExclusiveSum(cub_tmp, cub_bytes, vcnt, vbase, (int64_t)c.n + 1, st);
     k_item_fill<<<bs.g1, 256, 0, st>>>(c.off, c.in_off, c.n, bs.pc.E, vbase, items, acc);
+}
+
+// reset of the total and the queue head (acc[2], the item count, stays) -> [k0] persistent
+// count [k1]
+void enqueue_count(cudaStream_t st, const CountCsr &c, const BatchedShape &bs,
+                   const uint64_t *items, unsigned long long *acc, cudaEvent_t k0, cudaEvent_t k1,
+                   bool external_events) {
+    cudaMemsetAsync(acc, 0, 2 * sizeof(unsigned long long), st);
     if (k0) {
         if (external_events) cudaEventRecordWithFlags(k0, st, cudaEventRecordExternal);
         else cudaEventRecord(k0, st);
@@ -526,6 +533,23 @@ void enqueue_batched(cudaStream_t st, const CountCsr &c, const BatchedShape &bs,
 }
 
 constexpr uint64_t kBatchedKernels = 5;  // item counts, scan (init + sweep), item fill, count
+
+void enqueue_batched(cudaStream_t st, const CountCsr &c, const BatchedShape &bs, uint64_t *items,
+                     uint32_t *vcnt, void *cub_tmp, unsigned long long *acc) {
+    enqueue_items(st, c, bs, items, vcnt, cub_tmp, acc);
+    enqueue_count(st, c, bs, items, acc, nullptr, nullptr, false);
+}
+
+// A plan's items, built once when the plan is made (the counting form does not change while
+// the plan exists), so that a replay launches only the count. Ordering them heaviest first
+// by an estimated cost (elements streamed per item) was tried: 2.76 ms on R-MAT-21 against
+// 2.72 ms for descending rank order, which keeps the items of one vertex together.
+rtg_status plan_items(rtg_ctx *ctx, const CountCsr &c, const BatchedShape &bs, TcPlan *p) {
+    enqueue_items(ctx->stream, c, bs, p->items, p->vcnt, p->cub_tmp, p->acc);
+    ctx->launches += kBatchedKernels - 1;
+    RTG_CUDA(ctx, cudaGetLastError());
+    return RTG_OK;
+}
 
 rtg_status batched_plan(rtg_ctx *ctx, rtg_graph *g, TcPlan **out) {
     rtg_config cfg = effective_config(ctx);
@@ -557,10 +581,11 @@ rtg_status batched_plan(rtg_ctx *ctx, rtg_graph *g, TcPlan **out) {
     if ((e = cudaEventCreate(&p->k0)) != cudaSuccess ||
         (e = cudaEventCreate(&p->k1)) != cudaSuccess)
         return bail(cuda_fail(ctx, e, "event", __FILE__, __LINE__));
+    if ((s = plan_items(ctx, c, bs, p)) != RTG_OK) return bail(s);
     if ((e = cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal)) !=
         cudaSuccess)
         return bail(cuda_fail(ctx, e, "capture", __FILE__, __LINE__));
-    enqueue_batched(ctx->stream, c, bs, p->items, p->vcnt, p->cub_tmp, p->acc, p->k0, p->k1, true);
+    enqueue_count(ctx->stream, c, bs, p->items, p->acc, p->k0, p->k1, true);
     e = cudaStreamEndCapture(ctx->stream, &p->graph);
     if (e != cudaSuccess) return bail(cuda_fail(ctx, e, "end capture", __FILE__, __LINE__));
     if ((e = cudaGraphInstantiate(&p->exec, p->graph, 0)) != cudaSuccess)
@@ -719,7 +744,7 @@ rtg_status tc_launch_direct(rtg_ctx *ctx, rtg_graph *g, void *scratch, uint64_t 
         (reinterpret_cast<uintptr_t>(vcnt + 2 * (c.n + 1ull)) + 255) & ~(uintptr_t)255);
     if ((uint64_t)(static_cast<char *>(tmp) - p) + bs.cub_bytes > scratch_bytes)
         return fail(ctx, RTG_ERR_INVALID_ARG, "scratch too small for the count");
-    enqueue_batched(ctx->stream, c, bs, items, vcnt, tmp, acc, nullptr, nullptr, false);
+    enqueue_batched(ctx->stream, c, bs, items, vcnt, tmp, acc);
     RTG_CUDA(ctx, cudaGetLastError());
     ctx->launches += kBatchedKernels;
     RTG_CUDA(ctx, cudaMemcpyAsync(h_total, acc, 8, cudaMemcpyDeviceToHost, ctx->stream));
