@@ -548,6 +548,9 @@ rtg_status plan_items(rtg_ctx *ctx, const CountCsr &c, const BatchedShape &bs, T
     enqueue_items(ctx->stream, c, bs, p->items, p->vcnt, p->cub_tmp, p->acc);
     ctx->launches += kBatchedKernels - 1;
     RTG_CUDA(ctx, cudaGetLastError());
+    // the plan may be replayed on another context's stream (the serving engine's runs
+    // share a graph's plan): the items must be complete before the plan is handed out
+    RTG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
     return RTG_OK;
 }
 
