@@ -51,6 +51,7 @@ CLI_TOOLS = {
     "rt_intersection": "si_main.cpp",
     "convertor": "convertor_main.cpp",
     "s_generator": "s_generator_main.cpp",
+    "m_generator": "m_generator_main.cpp",
 }
 
 

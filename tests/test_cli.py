@@ -36,6 +36,19 @@ def test_s_generator_reproduces_reference_files(tmp_path, name):
     assert open(path, "rb").read() == (GOLDEN / "si" / f"{name}.s_data").read_bytes()
 
 
+@pytest.mark.parametrize("name", [n for n, r in si_golden().items() if r["mode"] == "si_multi"])
+def test_m_generator_reproduces_reference_files(tmp_path, name):
+    """Uniform, normal and exponential multi-set files, byte for byte as the reference's
+    generator wrote them (its fixed 1000 A sets replaced by the recorded count)."""
+    rec = si_golden()[name]
+    length, skew, sel, dist, lam, num_a, num_b = rec["args"]
+    out = run("m_generator", "-l", length, "-r", skew, "-s", sel, "-d", dist, "-b", lam,
+              "-a", num_a, "-n", num_b, "-f", str(tmp_path) + "/")
+    path = re.search(r"written to path: (\S+)", out).group(1)
+    assert path.endswith({"0": "_uni.m_data", "1": "_nor.m_data"}.get(dist, "_exp.m_data"))
+    assert open(path, "rb").read() == (GOLDEN / "si" / f"{name}.s_data").read_bytes()
+
+
 def test_convertor_matches_binary_writer(tmp_path):
     s, d = golden_edges(tc_golden()["wheel"])
     (tmp_path / "g.txt").write_text("".join(f"{a} {b}\n" for a, b in zip(s, d)))
