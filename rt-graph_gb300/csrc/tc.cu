@@ -240,7 +240,7 @@ __device__ __forceinline__ uint32_t stream_item(const uint32_t *__restrict__ adj
 #pragma unroll
         for (int j = 0; j < kLoads; ++j) b.w[j] = i + 32 * j < Y ? __ldg(adj + i + 32 * j) : idle;
         X += 32 * kLoads;
-        settle();
+        if (__builtin_expect(X >= Y, 0)) settle();  // once per in-edge: keep it off the block path
         return b;
     };
     settle();
