@@ -381,12 +381,12 @@ __global__ void k_tc_warp(const uint64_t *__restrict__ off, const uint32_t *__re
             const uint32_t mask = p.R - 1;
             cnt += stream_item_flat(adj, in_rng + kin, k0, k1, lane, [&](uint32_t w) -> uint32_t {
                 uint32_t sl = hash_slot(w, lg);
-                while (true) {
-                    const uint32_t x = reg[sl];
-                    if (x == w) return 1u;
-                    if (x == 0u) return 0u;
+                uint32_t x = reg[sl];
+                while (__builtin_expect(x != w && x != 0u, 0)) {
                     sl = (sl + 1) & mask;
+                    x = reg[sl];
                 }
+                return x == w ? 1u : 0u;
             });
         } else {
             for (uint32_t kk = k0; kk < k1; ++kk) {
