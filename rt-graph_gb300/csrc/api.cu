@@ -684,7 +684,6 @@ rtg_status rtg_tc_count_host_edges(rtg_ctx *ctx, const uint32_t *src, const uint
             cudaEventElapsedTime(&h2d, ctx->ev[6], ctx->ev[7]);
             t.h2d_ms = h2d;
             t.h2d_bytes = m * 8;
-            t.build_ms = now_ms() - t0 - t.h2d_ms;
             t.algo_bytes = 0;
             cudaError_t e = cudaEventRecord(ctx->ev[0], ctx->stream);
             if (e != cudaSuccess) s = cuda_fail(ctx, e, "event", __FILE__, __LINE__);
@@ -699,9 +698,11 @@ rtg_status rtg_tc_count_host_edges(rtg_ctx *ctx, const uint32_t *src, const uint
         tg.d_src = tg.d_dst = nullptr;  // borrowed scratch: nothing here is freed
         tg.cnt = CountCsr{};
         if (s != RTG_OK) return s;
-        float ms = 0;
+        float ms = 0, bms = 0;
         cudaEventElapsedTime(&ms, ctx->ev[0], ctx->ev[1]);
+        cudaEventElapsedTime(&bms, ctx->ev[7], ctx->ev[0]);  // device time of the build
         t.count_ms = t.main_kernel_ms = ms;
+        t.build_ms = bms;
         *out_total = h;
         t.d2h_bytes = 8;
         t.kernel_launches = ctx->launches - l0;

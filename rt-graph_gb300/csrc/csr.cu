@@ -414,11 +414,17 @@ __global__ void k_row_offsets32(const uint32_t *keys, uint64_t m, uint32_t n, ui
     }
 }
 
+// *num -= 1 when the last of the *num sorted distinct keys is the self-loop sentinel
+__global__ void k_unique_tail(int64_t *num, const uint64_t *keys, uint64_t sentinel) {
+    const int64_t k = *num;
+    if (k > 0 && keys[k - 1] == sentinel) *num = k - 1;
+}
+
 // Rows, in-edge suffix ranges and stats of the counting form from its rank edge keys
 // (sorted, unique, mr of them) in ek; `other` is a key buffer of mr entries and src_r one
 // of mr words.
 rtg_status count_tail(rtg_ctx *ctx, CountCsr &cc, uint64_t *ek, uint64_t *other, uint64_t mr,
-                      uint32_t n, int B, uint32_t *src_r) {
+                      uint32_t n, int B, uint32_t *src_r, bool stats = true) {
     cc.m = mr;
     if (mr == 0) {
         RTG_CUDA(ctx, cudaMemsetAsync(cc.off, 0, (n + 1ull) * 8, ctx->stream));
@@ -449,6 +455,11 @@ rtg_status count_tail(rtg_ctx *ctx, CountCsr &cc, uint64_t *ek, uint64_t *other,
                                                                             cc.in_off);
     ctx->launches += 2;
     RTG_CUDA(ctx, cudaGetLastError());
+    if (!stats) {  // max_deg stays 0: the one-shot count does not read it
+        cc.max_deg = 0;
+        cc.built = true;
+        return RTG_OK;
+    }
     unsigned long long *w = ctx->d_scalars;
     RTG_CUDA(ctx, cudaMemsetAsync(w, 0, 16, ctx->stream));
     k_stats<<<grid_for(ctx, n), kThreads, 0, ctx->stream>>>(cc.off, cc.adj, nullptr, mr, n, w,
@@ -626,19 +637,18 @@ rtg_status build_count_direct(rtg_ctx *ctx, rtg_graph *g, bool in_scratch, bool 
         RTG_CUDA(ctx, cub::DeviceSelect::Unique(tmp, bytes, de.Current(), de.Alternate(), d_num,
                                                 (int64_t)m, ctx->stream));
         ctx->launches += 2;
+        uint64_t *ek = de.Alternate(), *other = de.Current();
+        // distinct keys without the self-loop sentinel (it sorts last), read in one trip
+        k_unique_tail<<<1, 1, 0, ctx->stream>>>(d_num, ek, sentinel);
+        ctx->launches++;
+        RTG_CUDA(ctx, cudaGetLastError());
         int64_t nu = 0;
         RTG_CUDA(ctx, cudaMemcpyAsync(&nu, d_num, 8, cudaMemcpyDeviceToHost, ctx->stream));
         RTG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
-        uint64_t *ek = de.Alternate(), *other = de.Current();
-        if (nu > 0) {
-            uint64_t last = 0;
-            RTG_CUDA(ctx, cudaMemcpy(&last, ek + nu - 1, 8, cudaMemcpyDeviceToHost));
-            if (last == sentinel) --nu;
-        }
         RTG_TRY(in_scratch ? count_alloc_scratch(ctx, g->cnt, n, (uint64_t)nu)
                            : count_alloc(ctx, g->cnt, n, (uint64_t)nu));
         g->orient = RTG_ORIENT_DEGREE;
-        return count_tail(ctx, g->cnt, ek, other, (uint64_t)nu, n, B, src_r);
+        return count_tail(ctx, g->cnt, ek, other, (uint64_t)nu, n, B, src_r, !in_scratch);
     }
     uint64_t *ukeys = k0;
     uint64_t mu = 0;
