@@ -414,10 +414,64 @@ __global__ void k_row_offsets32(const uint32_t *keys, uint64_t m, uint32_t n, ui
     }
 }
 
-// *num -= 1 when the last of the *num sorted distinct keys is the self-loop sentinel
-__global__ void k_unique_tail(int64_t *num, const uint64_t *keys, uint64_t sentinel) {
-    const int64_t k = *num;
-    if (k > 0 && keys[k - 1] == sentinel) *num = k - 1;
+rtg_status in_edge_tail(rtg_ctx *ctx, CountCsr &cc, uint64_t *ek, uint64_t *other, uint64_t mr,
+                        uint32_t n, int B, uint32_t *src_r, bool stats);
+
+// Stable sort of 32-bit (key, value) pairs over the low `bits` key bits.
+rtg_status sort_pairs32(rtg_ctx *ctx, cub::DoubleBuffer<uint32_t> &k,
+                        cub::DoubleBuffer<uint32_t> &v, uint64_t m, int bits) {
+    if (m < 2) return RTG_OK;
+    size_t bytes = 0;
+    RTG_CUDA(ctx, cub::DeviceRadixSort::SortPairs(nullptr, bytes, k, v, (int64_t)m, 0, bits,
+                                                  ctx->stream));
+    void *tmp = nullptr;
+    RTG_TRY(scratch(ctx, 0, bytes, &tmp));
+    RTG_CUDA(ctx, cub::DeviceRadixSort::SortPairs(tmp, bytes, k, v, (int64_t)m, 0, bits,
+                                                  ctx->stream));
+    ctx->launches += (bits + 7) / 8 + 1;
+    return RTG_OK;
+}
+
+rtg_status exclusive_sum_u32(rtg_ctx *ctx, const uint32_t *in, uint32_t *out, uint64_t k) {
+    size_t bytes = 0;
+    RTG_CUDA(ctx, cub::DeviceScan::ExclusiveSum(nullptr, bytes, in, out, (int64_t)k, ctx->stream));
+    void *tmp = nullptr;
+    RTG_TRY(scratch(ctx, 0, bytes, &tmp));
+    RTG_CUDA(ctx, cub::DeviceScan::ExclusiveSum(tmp, bytes, in, out, (int64_t)k, ctx->stream));
+    ctx->launches += 2;
+    return RTG_OK;
+}
+
+// (higher rank, lower rank) of every input edge; a self loop gets (n, n), which sorts last
+__global__ void k_rank_pairs(const uint32_t *s, const uint32_t *d, uint64_t m,
+                             const uint32_t *rank, uint32_t n, uint32_t *hi, uint32_t *lo) {
+    GRID_STRIDE(i, m) {
+        const uint32_t a = rank[s[i]], b = rank[d[i]];
+        hi[i] = a == b ? n : max(a, b);
+        lo[i] = a == b ? n : min(a, b);
+    }
+}
+
+// keep[e] = 1 for the first copy of every edge in (lower, higher) order, 0 for its
+// duplicates and for self loops; keep[m] = 0
+__global__ void k_keep_flags(const uint32_t *lo, const uint32_t *hi, uint64_t m, uint32_t n,
+                             uint32_t *keep) {
+    GRID_STRIDE(e, m + 1) {
+        uint32_t k = 0;
+        if (e < m && lo[e] < n) k = (e == 0 || lo[e - 1] != lo[e] || hi[e - 1] != hi[e]) ? 1u : 0u;
+        keep[e] = k;
+    }
+}
+
+// the kept edges to their rows: adj[pos[e]] = higher endpoint, src[pos[e]] = lower one
+__global__ void k_compact_rows(const uint32_t *lo, const uint32_t *hi, const uint32_t *keep,
+                               const uint32_t *pos, uint64_t m, uint32_t *adj, uint32_t *src) {
+    GRID_STRIDE(e, m) {
+        if (keep[e]) {
+            adj[pos[e]] = hi[e];
+            src[pos[e]] = lo[e];
+        }
+    }
 }
 
 // Rows, in-edge suffix ranges and stats of the counting form from its rank edge keys
@@ -434,11 +488,20 @@ rtg_status count_tail(rtg_ctx *ctx, CountCsr &cc, uint64_t *ek, uint64_t *other,
     }
     k_csr_fill<<<grid_for(ctx, mr), kThreads, 0, ctx->stream>>>(ek, mr, B, cc.adj, src_r);
     k_row_offsets<<<grid_for(ctx, n + 1ull), kThreads, 0, ctx->stream>>>(ek, mr, B, n, cc.off);
-    // ek is free once rows are filled: the pair sort ping-pongs between `other` and ek
+    ctx->launches += 2;
+    // ek is free once rows are filled
+    return in_edge_tail(ctx, cc, ek, other, mr, n, B, src_r, stats);
+}
+
+// In-edge suffix ranges and stats of a counting form whose rows (cc.off, cc.adj, and the
+// row of every position in src_r) are filled: ek and other are scratch of mr u64 each, for
+// the pair sort that groups the in-edges by head.
+rtg_status in_edge_tail(rtg_ctx *ctx, CountCsr &cc, uint64_t *ek, uint64_t *other, uint64_t mr,
+                        uint32_t n, int B, uint32_t *src_r, bool stats) {
     uint32_t *ka = reinterpret_cast<uint32_t *>(other), *pa = ka + mr;
     uint32_t *kb = reinterpret_cast<uint32_t *>(ek), *pb = kb + mr;
     k_in_pairs<<<grid_for(ctx, mr), kThreads, 0, ctx->stream>>>(cc.adj, mr, cc.off, ka, pa, src_r);
-    ctx->launches += 3;
+    ctx->launches++;
     RTG_CUDA(ctx, cudaGetLastError());
     cub::DoubleBuffer<uint32_t> dk(ka, kb), dv(pa, pb);
     size_t bytes = 0;
@@ -620,35 +683,51 @@ rtg_status build_count_direct(rtg_ctx *ctx, rtg_graph *g, bool in_scratch, bool 
         RTG_CUDA(ctx, cudaGetLastError());
         cub::DoubleBuffer<uint64_t> dr(r0, r1);
         RTG_TRY(radix_sort(ctx, dr, n, std::min(64, B + 32)));
-        const uint64_t sentinel = (uint64_t)n << B;
         k_rank_scatter<<<grid_for(ctx, n), kThreads, 0, ctx->stream>>>(dr.Current(), n, B, rank);
-        k_rank_edge_keys<<<grid_for(ctx, m), kThreads, 0, ctx->stream>>>(g->d_src, g->d_dst, m,
-                                                                          rank, B, sentinel, k0);
-        ctx->launches += 2;
-        RTG_CUDA(ctx, cudaGetLastError());
-        cub::DoubleBuffer<uint64_t> de(k0, k1);
-        RTG_TRY(radix_sort(ctx, de, m, std::min(64, 2 * B)));  // n < 2^B: the sentinel fits
-        int64_t *d_num = (int64_t *)(ctx->d_scalars + 4);
-        size_t bytes = 0;
-        RTG_CUDA(ctx, cub::DeviceSelect::Unique(nullptr, bytes, de.Current(), de.Alternate(),
-                                                d_num, (int64_t)m, ctx->stream));
-        void *tmp = nullptr;
-        RTG_TRY(scratch(ctx, 0, bytes, &tmp));
-        RTG_CUDA(ctx, cub::DeviceSelect::Unique(tmp, bytes, de.Current(), de.Alternate(), d_num,
-                                                (int64_t)m, ctx->stream));
-        ctx->launches += 2;
-        uint64_t *ek = de.Alternate(), *other = de.Current();
-        // distinct keys without the self-loop sentinel (it sorts last), read in one trip
-        k_unique_tail<<<1, 1, 0, ctx->stream>>>(d_num, ek, sentinel);
+        ctx->launches++;
+        // (lower, higher) order from two stable sorts of 32-bit pairs, least significant key
+        // first: by the higher endpoint, then by the lower one (a sort of the 64-bit keys
+        // (lower << B | higher) orders them the same, at twice the bytes per pass); self
+        // loops carry (n, n) and sort last, the copies of an edge end up adjacent
+        uint32_t *A = reinterpret_cast<uint32_t *>(k0), *C = A + cap;
+        uint32_t *Bv = reinterpret_cast<uint32_t *>(k1), *D = Bv + cap;
+        k_rank_pairs<<<grid_for(ctx, m), kThreads, 0, ctx->stream>>>(g->d_src, g->d_dst, m, rank,
+                                                                      n, A, Bv);
         ctx->launches++;
         RTG_CUDA(ctx, cudaGetLastError());
-        int64_t nu = 0;
-        RTG_CUDA(ctx, cudaMemcpyAsync(&nu, d_num, 8, cudaMemcpyDeviceToHost, ctx->stream));
-        RTG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
-        RTG_TRY(in_scratch ? count_alloc_scratch(ctx, g->cnt, n, (uint64_t)nu)
-                           : count_alloc(ctx, g->cnt, n, (uint64_t)nu));
+        cub::DoubleBuffer<uint32_t> kh(A, C), vl(Bv, D);
+        RTG_TRY(sort_pairs32(ctx, kh, vl, m, B));
+        cub::DoubleBuffer<uint32_t> kl(vl.Current(), vl.Alternate()), vh(kh.Current(), kh.Alternate());
+        RTG_TRY(sort_pairs32(ctx, kl, vh, m, B));
+        const uint32_t *lo = kl.Current(), *hi = vh.Current();
+        uint32_t *keep, *pos;
+        RTG_TRY(buf.alloc(&keep, m + 1));
+        RTG_TRY(buf.alloc(&pos, m + 1));
+        k_keep_flags<<<grid_for(ctx, m + 1), kThreads, 0, ctx->stream>>>(lo, hi, m, n, keep);
+        ctx->launches++;
+        RTG_CUDA(ctx, cudaGetLastError());
+        RTG_TRY(exclusive_sum_u32(ctx, keep, pos, m + 1));
+        uint32_t mr = 0;
+        RTG_TRY(read_u32(ctx, pos + m, &mr));
+        RTG_TRY(in_scratch ? count_alloc_scratch(ctx, g->cnt, n, mr)
+                           : count_alloc(ctx, g->cnt, n, mr));
         g->orient = RTG_ORIENT_DEGREE;
-        return count_tail(ctx, g->cnt, ek, other, (uint64_t)nu, n, B, src_r, !in_scratch);
+        CountCsr &cc = g->cnt;
+        cc.m = mr;
+        k_compact_rows<<<grid_for(ctx, m), kThreads, 0, ctx->stream>>>(lo, hi, keep, pos, m,
+                                                                        cc.adj, src_r);
+        k_row_offsets32<<<grid_for(ctx, n + 1ull), kThreads, 0, ctx->stream>>>(src_r, mr, n,
+                                                                                cc.off);
+        ctx->launches += 2;
+        RTG_CUDA(ctx, cudaGetLastError());
+        if (mr == 0) {
+            RTG_CUDA(ctx, cudaMemsetAsync(cc.in_off, 0, (n + 1ull) * 8, ctx->stream));
+            cc.built = true;
+            return RTG_OK;
+        }
+        // the sorted pairs are dead once the rows are filled: their buffers hold the in-edge
+        // pair sort
+        return in_edge_tail(ctx, cc, k0, k1, mr, n, B, src_r, !in_scratch);
     }
     uint64_t *ukeys = k0;
     uint64_t mu = 0;
