@@ -417,6 +417,15 @@ __global__ void k_row_offsets32(const uint32_t *keys, uint64_t m, uint32_t n, ui
 rtg_status in_edge_tail(rtg_ctx *ctx, CountCsr &cc, uint64_t *ek, uint64_t *other, uint64_t mr,
                         uint32_t n, int B, uint32_t *src_r, bool stats);
 
+__global__ void k_iota32(uint32_t *p, uint64_t n) {
+    GRID_STRIDE(i, n) { p[i] = (uint32_t)i; }
+}
+
+// rank[ids[i]] = i for the ids in rank order
+__global__ void k_rank_scatter32(const uint32_t *ids, uint32_t n, uint32_t *rank) {
+    GRID_STRIDE(i, (uint64_t)n) { rank[ids[i]] = (uint32_t)i; }
+}
+
 // Stable sort of 32-bit (key, value) pairs over the low `bits` key bits.
 rtg_status sort_pairs32(rtg_ctx *ctx, cub::DoubleBuffer<uint32_t> &k,
                         cub::DoubleBuffer<uint32_t> &v, uint64_t m, int bits) {
@@ -678,12 +687,16 @@ rtg_status build_count_direct(rtg_ctx *ctx, rtg_graph *g, bool in_scratch, bool 
                 g->d_src, g->d_dst, m, stride, deg);
             ctx->launches++;
         }
-        k_rank_keys<<<grid_for(ctx, n), kThreads, 0, ctx->stream>>>(deg, n, B, r0);
+        // (degree, id) order: a stable sort of the ids, ascending, by degree (32-bit pairs:
+        // the order a sort of the 64-bit keys degree << B | id gives, at fewer bytes)
+        uint32_t *ids = reinterpret_cast<uint32_t *>(r1), *ids_alt = ids + (n + 1ull);
+        uint32_t *deg_alt = reinterpret_cast<uint32_t *>(r0);
+        k_iota32<<<grid_for(ctx, n), kThreads, 0, ctx->stream>>>(ids, n);
         ctx->launches++;
         RTG_CUDA(ctx, cudaGetLastError());
-        cub::DoubleBuffer<uint64_t> dr(r0, r1);
-        RTG_TRY(radix_sort(ctx, dr, n, std::min(64, B + 32)));
-        k_rank_scatter<<<grid_for(ctx, n), kThreads, 0, ctx->stream>>>(dr.Current(), n, B, rank);
+        cub::DoubleBuffer<uint32_t> dk(deg, deg_alt), dv(ids, ids_alt);
+        RTG_TRY(sort_pairs32(ctx, dk, dv, n, 32));
+        k_rank_scatter32<<<grid_for(ctx, n), kThreads, 0, ctx->stream>>>(dv.Current(), n, rank);
         ctx->launches++;
         // (lower, higher) order from two stable sorts of 32-bit pairs, least significant key
         // first: by the higher endpoint, then by the lower one (a sort of the 64-bit keys
