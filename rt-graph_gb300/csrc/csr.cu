@@ -667,8 +667,10 @@ rtg_status build_count_direct(rtg_ctx *ctx, rtg_graph *g, bool in_scratch, bool 
     RTG_TRY(buf.alloc(&k0, cap));
     RTG_TRY(buf.alloc(&k1, cap));
     if (raw_degree && m) {
-        // ranks by degree in the input list (duplicates and self loops counted); the one
-        // sort of the rank edge keys then also brings duplicates together for Unique
+        // row positions and the row count below are 32-bit
+        if (m > 0xFFFFFFFFull)
+            return fail(ctx, RTG_ERR_INVALID_ARG, "one-shot count takes at most 2^32 - 1 edges");
+        // ranks by degree in the input list (duplicates and self loops counted)
         RTG_TRY(buf.alloc(&rank, n));
         RTG_TRY(buf.alloc(&r0, n + 1ull));
         RTG_TRY(buf.alloc(&r1, n + 1ull));

@@ -207,6 +207,38 @@ def test_one_shot_pinned_edges_pulled(ctx):
             assert t.h2d_bytes == 8 * len(s)
 
 
+@pytest.mark.parametrize("row", [32, 33, 2048, 2049, 5000])
+def test_one_shot_long_raw_rows(ctx, row):
+    """One-shot build on raw rows (edge copies included) of 32, 33, 2048, 2049 and 5000
+    entries, around the warp, block and sort-pass sizes: vertex 0 gets exactly `row` raw
+    entries (repeated edges to 60 hubs of a clique whose leaves give them higher degrees);
+    a second vertex adds 700 copies of edges to 20 of the hubs. Pageable and page-locked
+    edges; counts agree with the oracle on the deduplicated graph."""
+    rng = np.random.default_rng(row)
+    hubs = np.arange(1, 61, dtype=np.uint32)
+    iu, ju = np.triu_indices(len(hubs), 1)
+    s = [hubs[iu], np.zeros(row, np.uint32), np.full(700, 100, np.uint32)]
+    d = [hubs[ju], rng.choice(hubs, row).astype(np.uint32),
+         rng.choice(hubs[:20], 700).astype(np.uint32)]
+    leaves = np.arange(1000, 1000 + len(hubs) * (row + 5), dtype=np.uint32)
+    s.append(np.repeat(hubs, row + 5))
+    d.append(leaves)
+    s, d = np.concatenate(s), np.concatenate(d)
+    perm = rng.permutation(len(s))
+    s, d = s[perm], d[perm]
+    flip = rng.random(len(s)) < 0.5
+    s, d = np.where(flip, d, s).astype(np.uint32), np.where(flip, s, d).astype(np.uint32)
+    off, adj = oracle.degree_csr(s, d)
+    want = oracle.tc_merge(off, adj)
+    hs = ctx.host_array(len(s), np.uint32)
+    hd = ctx.host_array(len(d), np.uint32)
+    hs[:] = s
+    hd[:] = d
+    for src, dst in ((s, d), (hs, hd)):
+        got, _ = ctx.tc_count_host_edges(src, dst, rtg.ORIENT_DEGREE, rtg.TC_BATCHED)
+        assert got == want, row
+
+
 def test_file_formats(ctx, tmp_path):
     rec = TC["wheel"]
     s, d = golden_edges(rec)
