@@ -18,6 +18,7 @@
 //                    self loops removed (graph.cpp:160-173), CSR (graph.cpp:71-102).
 //  SYMMETRIC       – simple graph with both directions stored.
 #include <cub/cub.cuh>
+#include <thrust/iterator/zip_iterator.h>
 
 #include <algorithm>
 
@@ -384,20 +385,46 @@ __global__ void k_rank_canon_keys(const uint64_t *ukeys, uint64_t m, int B, cons
 // stay ascending within a head. The row end of every position replaces its row id in
 // src_r here, where the rows are read in order, so that the fill after the sort reads one
 // scattered word per in-edge instead of two dependent ones.
-__global__ void k_in_pairs(const uint32_t *adj_r, uint64_t m, const uint64_t *off_r,
-                           uint32_t *keys, uint32_t *pos, uint32_t *src_r) {
-    GRID_STRIDE(e, m) {
-        keys[e] = adj_r[e];
-        pos[e] = (uint32_t)e;
-        src_r[e] = (uint32_t)off_r[src_r[e] + 1];
+__global__ void k_in_pairs(const uint32_t *__restrict__ adj_r, uint64_t m,
+                           const uint64_t *__restrict__ off_r, uint32_t *__restrict__ keys,
+                           uint32_t *__restrict__ pos, uint32_t *__restrict__ src_r) {
+    const uint64_t T = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t e0 = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; e0 < m; e0 += 4 * T) {
+        uint32_t w[4], r[4];
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            const uint64_t e = e0 + k * T;
+            w[k] = e < m ? adj_r[e] : 0u;
+            r[k] = e < m ? src_r[e] : 0u;
+        }
+#pragma unroll
+        for (int k = 0; k < 4; ++k) r[k] = (uint32_t)__ldg(off_r + r[k] + 1);
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            const uint64_t e = e0 + k * T;
+            if (e < m) {
+                keys[e] = w[k];
+                pos[e] = (uint32_t)e;
+                src_r[e] = r[k];
+            }
+        }
     }
 }
 
-// rng[i] = [e + 1, end of e's row) for the in-edge at position e (rend: row end per position)
-__global__ void k_in_fill(const uint32_t *pos, uint64_t m, const uint32_t *rend, uint2 *rng) {
-    GRID_STRIDE(i, m) {
-        const uint32_t e = pos[i];
-        rng[i] = make_uint2(e + 1, rend[e]);
+// rng[i] = [e + 1, end of e's row) for the in-edge at position e (rend: row end per position);
+// four in-edges per thread, a grid's width apart
+__global__ void k_in_fill(const uint32_t *__restrict__ pos, uint64_t m,
+                          const uint32_t *__restrict__ rend, uint2 *__restrict__ rng) {
+    const uint64_t T = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t i0 = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i0 < m; i0 += 4 * T) {
+        uint32_t e[4], r[4];
+#pragma unroll
+        for (int k = 0; k < 4; ++k) e[k] = i0 + k * T < m ? __ldg(pos + i0 + k * T) : 0u;
+#pragma unroll
+        for (int k = 0; k < 4; ++k) r[k] = __ldg(rend + e[k]);
+#pragma unroll
+        for (int k = 0; k < 4; ++k)
+            if (i0 + k * T < m) rng[i0 + k * T] = make_uint2(e[k] + 1, r[k]);
     }
 }
 
@@ -441,46 +468,46 @@ rtg_status sort_pairs32(rtg_ctx *ctx, cub::DoubleBuffer<uint32_t> &k,
     return RTG_OK;
 }
 
-rtg_status exclusive_sum_u32(rtg_ctx *ctx, const uint32_t *in, uint32_t *out, uint64_t k) {
-    size_t bytes = 0;
-    RTG_CUDA(ctx, cub::DeviceScan::ExclusiveSum(nullptr, bytes, in, out, (int64_t)k, ctx->stream));
-    void *tmp = nullptr;
-    RTG_TRY(scratch(ctx, 0, bytes, &tmp));
-    RTG_CUDA(ctx, cub::DeviceScan::ExclusiveSum(tmp, bytes, in, out, (int64_t)k, ctx->stream));
-    ctx->launches += 2;
-    return RTG_OK;
-}
-
-// (higher rank, lower rank) of every input edge; a self loop gets (n, n), which sorts last
-__global__ void k_rank_pairs(const uint32_t *s, const uint32_t *d, uint64_t m,
-                             const uint32_t *rank, uint32_t n, uint32_t *hi, uint32_t *lo) {
-    GRID_STRIDE(i, m) {
-        const uint32_t a = rank[s[i]], b = rank[d[i]];
-        hi[i] = a == b ? n : max(a, b);
-        lo[i] = a == b ? n : min(a, b);
-    }
-}
-
-// keep[e] = 1 for the first copy of every edge in (lower, higher) order, 0 for its
-// duplicates and for self loops; keep[m] = 0
-__global__ void k_keep_flags(const uint32_t *lo, const uint32_t *hi, uint64_t m, uint32_t n,
-                             uint32_t *keep) {
-    GRID_STRIDE(e, m + 1) {
-        uint32_t k = 0;
-        if (e < m && lo[e] < n) k = (e == 0 || lo[e - 1] != lo[e] || hi[e - 1] != hi[e]) ? 1u : 0u;
-        keep[e] = k;
-    }
-}
-
-// the kept edges to their rows: adj[pos[e]] = higher endpoint, src[pos[e]] = lower one
-__global__ void k_compact_rows(const uint32_t *lo, const uint32_t *hi, const uint32_t *keep,
-                               const uint32_t *pos, uint64_t m, uint32_t *adj, uint32_t *src) {
-    GRID_STRIDE(e, m) {
-        if (keep[e]) {
-            adj[pos[e]] = hi[e];
-            src[pos[e]] = lo[e];
+// (higher rank, lower rank) of every input edge; a self loop gets (n, n), which sorts last.
+// Four edges per thread, a grid's width apart, so that their loads and rank gathers are in
+// flight together.
+__global__ void k_rank_pairs(const uint32_t *__restrict__ s, const uint32_t *__restrict__ d,
+                             uint64_t m, const uint32_t *__restrict__ rank, uint32_t n,
+                             uint32_t *__restrict__ hi, uint32_t *__restrict__ lo) {
+    const uint64_t T = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t i0 = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i0 < m; i0 += 4 * T) {
+        uint32_t x[4], y[4];
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            const uint64_t i = i0 + k * T;
+            x[k] = i < m ? __ldg(s + i) : 0u;
+            y[k] = i < m ? __ldg(d + i) : 0u;
+        }
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            x[k] = __ldg(rank + x[k]);
+            y[k] = __ldg(rank + y[k]);
+        }
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            const uint64_t i = i0 + k * T;
+            if (i < m) {
+                hi[i] = x[k] == y[k] ? n : max(x[k], y[k]);
+                lo[i] = x[k] == y[k] ? n : min(x[k], y[k]);
+            }
         }
     }
+}
+
+// After the unique pass over the sorted (lower, higher) pairs (*num runs kept): the rows end
+// before the (n, n) entry the self loops leave last, if any; *mr = the row entries, and the
+// kAdjPadBytes after them are zeroed.
+__global__ void k_unique_rows_end(const int64_t *num, const uint32_t *src, uint32_t *adj,
+                                  uint32_t n, uint32_t *mr) {
+    const int64_t k = *num;
+    const uint64_t r = (k > 0 && src[k - 1] == n) ? (uint64_t)(k - 1) : (uint64_t)k;
+    for (uint32_t q = threadIdx.x; q < kAdjPadBytes / 4; q += blockDim.x) adj[r + q] = 0u;
+    if (threadIdx.x == 0) *mr = (uint32_t)r;
 }
 
 // Rows, in-edge suffix ranges and stats of the counting form from its rank edge keys
@@ -715,25 +742,35 @@ rtg_status build_count_direct(rtg_ctx *ctx, rtg_graph *g, bool in_scratch, bool 
         cub::DoubleBuffer<uint32_t> kl(vl.Current(), vl.Alternate()), vh(kh.Current(), kh.Alternate());
         RTG_TRY(sort_pairs32(ctx, kl, vh, m, B));
         const uint32_t *lo = kl.Current(), *hi = vh.Current();
-        uint32_t *keep, *pos;
-        RTG_TRY(buf.alloc(&keep, m + 1));
-        RTG_TRY(buf.alloc(&pos, m + 1));
-        k_keep_flags<<<grid_for(ctx, m + 1), kThreads, 0, ctx->stream>>>(lo, hi, m, n, keep);
-        ctx->launches++;
-        RTG_CUDA(ctx, cudaGetLastError());
-        RTG_TRY(exclusive_sum_u32(ctx, keep, pos, m + 1));
-        uint32_t mr = 0;
-        RTG_TRY(read_u32(ctx, pos + m, &mr));
-        RTG_TRY(in_scratch ? count_alloc_scratch(ctx, g->cnt, n, mr)
-                           : count_alloc(ctx, g->cnt, n, mr));
+        // the rows are sized for every input edge (copies included) and trimmed to the
+        // unique ones below
+        RTG_TRY(in_scratch ? count_alloc_scratch(ctx, g->cnt, n, m)
+                           : count_alloc(ctx, g->cnt, n, m));
         g->orient = RTG_ORIENT_DEGREE;
         CountCsr &cc = g->cnt;
+        // the copies of an edge are adjacent: one pass keeps the first pair of every run as
+        // a row entry (src = lower, adj = higher); the self loops' (n, n) pairs sort last
+        // and leave one entry there, which k_unique_rows_end drops
+        int64_t *d_num = reinterpret_cast<int64_t *>(ctx->d_scalars + 4);
+        uint32_t *d_mr = reinterpret_cast<uint32_t *>(ctx->d_scalars + 12);
+        auto pin = thrust::make_zip_iterator(lo, hi);
+        auto pout = thrust::make_zip_iterator(src_r, cc.adj);
+        size_t ubytes = 0;
+        RTG_CUDA(ctx, cub::DeviceSelect::Unique(nullptr, ubytes, pin, pout, d_num, (int64_t)m,
+                                                ctx->stream));
+        void *utmp = nullptr;
+        RTG_TRY(scratch(ctx, 0, ubytes, &utmp));
+        RTG_CUDA(ctx, cub::DeviceSelect::Unique(utmp, ubytes, pin, pout, d_num, (int64_t)m,
+                                                ctx->stream));
+        k_unique_rows_end<<<1, 32, 0, ctx->stream>>>(d_num, src_r, cc.adj, n, d_mr);
+        ctx->launches += 3;
+        RTG_CUDA(ctx, cudaGetLastError());
+        uint32_t mr = 0;
+        RTG_TRY(read_u32(ctx, d_mr, &mr));
         cc.m = mr;
-        k_compact_rows<<<grid_for(ctx, m), kThreads, 0, ctx->stream>>>(lo, hi, keep, pos, m,
-                                                                        cc.adj, src_r);
         k_row_offsets32<<<grid_for(ctx, n + 1ull), kThreads, 0, ctx->stream>>>(src_r, mr, n,
                                                                                 cc.off);
-        ctx->launches += 2;
+        ctx->launches++;
         RTG_CUDA(ctx, cudaGetLastError());
         if (mr == 0) {
             RTG_CUDA(ctx, cudaMemsetAsync(cc.in_off, 0, (n + 1ull) * 8, ctx->stream));
