@@ -625,7 +625,7 @@ def run_gpu(args, dist: Dist) -> None:
     roofline.update(dram_view(roofline["traffic"], kms, peaks["hbm_gbs"],
                               "the formula charges both full out-lists of every oriented edge; "
                               "the kernel streams only in-edge suffixes (2.98e9 elements) "
-                              "against shared-memory bitmaps: issue-bound (82 % issue-active "
+                              "against shared-memory bitmaps: issue-bound (84 % issue-active "
                               "by ncu), DRAM traffic below"))
     cpu = None
     if dist.rank == 0 and dist.ws == 1 and not args.no_cpu_baseline:
