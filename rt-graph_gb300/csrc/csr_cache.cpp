@@ -26,7 +26,7 @@ namespace {
 
 constexpr char kMagic[8] = {'R', 'T', 'G', 'C', 'S', 'R', '0', '1'};
 constexpr uint32_t kVersion = 1;
-enum : uint32_t { kPartOri = 1, kPartCnt = 2, kPartSym = 4 };
+constexpr uint32_t kPartOri = 1, kPartCnt = 2, kPartSym = 4;
 
 struct Writer {
     FILE *f;
