@@ -124,6 +124,31 @@ def test_batched_schedules_agree(ctx, cfg):
         ctx.set_config(**old.as_dict())
 
 
+def test_slot_and_ratio_boundaries(ctx):
+    """Default batched schedule (4 KB slots: 1024 words for both widened lists and their
+    sentinels; search ratio 8): pairs whose words land just under, on and just over one
+    slot, for every 16-byte alignment of either list's start, and pairs on either side of
+    |B| = 8 |A| both inside one slot and beyond it. Counts agree with the oracle."""
+    rng = np.random.default_rng(17)
+    lists = []
+    for pad in range(4):  # a list of `pad` elements shifts the next list's alignment
+        if pad:
+            lists.append(np.sort(rng.choice(1 << 20, pad, replace=False)).astype(np.uint32))
+        for n in (500, 503, 504, 505, 506, 507, 508, 509, 510, 511, 512, 513, 1016, 1017):
+            lists.append(np.sort(rng.choice(1 << 12, n, replace=False)).astype(np.uint32))
+    for a in (40, 200):  # ratio 8 in a slot (40 x 320 / 321), beyond a slot (200 x 1600 / 1601)
+        base = np.sort(rng.choice(1 << 16, 8 * a + 1, replace=False)).astype(np.uint32)
+        lists += [base[::8][:a].copy(), base[: 8 * a].copy(), base.copy()]
+    off = np.zeros(len(lists) + 1, np.uint64)
+    off[1:] = np.cumsum([len(x) for x in lists])
+    el = np.concatenate(lists).astype(np.uint32)
+    k = len(lists)
+    pa, pb = np.meshgrid(np.arange(k, dtype=np.uint32), np.arange(k, dtype=np.uint32))
+    pa, pb = pa.ravel(), pb.ravel()
+    got, _ = ctx.sets(off, el).count(pa, pb, rtg.SI_AUTO)
+    assert np.array_equal(got, oracle.si_pairs(off, el, pa, pb))
+
+
 def test_config3_full_size_known_answers(ctx):
     """10^6 lognormal pairs (median 64, sigma 1.5, lengths in [1, 65536], universe 2^26)."""
     off, el, pa, pb, exp = rtg.gen_si_pairs(1_000_000, seed=1)
