@@ -207,6 +207,26 @@ def test_one_shot_pinned_edges_pulled(ctx):
             assert t.h2d_bytes == 8 * len(s)
 
 
+def test_one_shot_degenerate_edge_lists(ctx):
+    """rtg_tc_count_host_edges on lists whose rows come out empty or tiny: no edges, only
+    self loops (their pairs are the only ones left after the copies go), only copies of one
+    edge, and small cliques buried in copies, reversed copies and self loops."""
+    tri = [(0, 1), (1, 2), (2, 0)]
+    k4 = [(i, j) for i in range(4) for j in range(i + 1, 4)]
+    cases = [
+        ([], 0), ([(5, 5)], 0), ([(1, 1), (2, 2), (3, 3)], 0), ([(0, 1)] * 10, 0),
+        (tri * 3 + [(b, a) for a, b in tri] + [(0, 0), (2, 2)], 1),
+        (k4 * 2 + [(7, 7)] + [(b, a) for a, b in k4], 4),
+        ([(9, 3), (3, 9), (9, 3)] + [(3 + i, 3 + j) for i, j in k4], 4),
+    ]
+    for edges, want in cases:
+        s = np.array([a for a, _ in edges], np.uint32)
+        d = np.array([b for _, b in edges], np.uint32)
+        for mode in MODES:
+            got, _ = ctx.tc_count_host_edges(s, d, rtg.ORIENT_DEGREE, mode)
+            assert got == want, (edges, mode)
+
+
 @pytest.mark.parametrize("row", [32, 33, 2048, 2049, 5000])
 def test_one_shot_long_raw_rows(ctx, row):
     """One-shot build on raw rows (edge copies included) of 32, 33, 2048, 2049 and 5000
