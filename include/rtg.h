@@ -226,7 +226,8 @@ rtg_status rtg_tc_count(rtg_ctx *ctx, rtg_graph *g, rtg_tc_mode mode, uint64_t *
  * RTG_TC_BATCHED the edges, the counting form and the count's buffers are kept in the
  * context's grow-only scratch (about 21 bytes per edge, released by rtg_destroy), so
  * repeated calls allocate nothing once it has grown; that form takes at most 2^32 - 1
- * edges (RTG_ERR_INVALID_ARG above). */
+ * edges and vertex ids below 2^31 - 1 (RTG_ERR_INVALID_ARG otherwise, before anything is
+ * sized by the ids). */
 rtg_status rtg_tc_count_host_edges(rtg_ctx *ctx, const uint32_t *src, const uint32_t *dst,
                                    uint64_t m, rtg_orient orient, rtg_tc_mode mode,
                                    uint64_t *out_total, rtg_timing *timing);

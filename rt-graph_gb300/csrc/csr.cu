@@ -658,6 +658,11 @@ rtg_status build_count_direct(rtg_ctx *ctx, rtg_graph *g, bool in_scratch, bool 
         if (maxid == kEmpty)
             return fail(ctx, RTG_ERR_INVALID_ARG, "vertex id 0xFFFFFFFF is reserved");
     }
+    // the arrays below are sized by the largest id, and the count takes fewer than 2^31
+    // vertices: refuse larger ids before allocating for them
+    if (m && maxid > 0x7FFFFFFEu)
+        return fail(ctx, RTG_ERR_INVALID_ARG,
+                    "vertex ids must be below 2^31 - 1 for a one-shot count (largest %u)", maxid);
     const uint32_t n = m ? maxid + 1 : 0;
     const int B = bits_for(maxid + 1ull);
     Buffers buf{ctx, {}};

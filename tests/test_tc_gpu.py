@@ -286,9 +286,17 @@ def test_errors_are_status_codes(ctx):
     with pytest.raises(rtg.RtgError) as e:   # unsorted row
         ctx.graph_from_csr(np.array([0, 2, 2, 2], np.int32), np.array([2, 1], np.int32))
     assert e.value.status == rtg.ERR_INVALID_ARG
+    # one-shot count: ids of 2^31 - 1 and above are refused before anything is sized by them
+    for big in (0x7FFFFFFF, 0x80000000, 0xFFFFFFFE, 0xFFFFFFFF):
+        with pytest.raises(rtg.RtgError) as e:
+            ctx.tc_count_host_edges(np.array([0, 1], np.uint32), np.array([1, big], np.uint32),
+                                    rtg.ORIENT_DEGREE, rtg.TC_BATCHED)
+        assert e.value.status == rtg.ERR_INVALID_ARG
     # the context is still usable after errors
     assert ctx.graph_from_edges(np.array([0, 1, 2], np.uint32),
                                 np.array([1, 2, 0], np.uint32)).build().tc()[0] == 1
+    s, d = np.array([0, 1, 2], np.uint32), np.array([1, 2, 0], np.uint32)
+    assert ctx.tc_count_host_edges(s, d, rtg.ORIENT_DEGREE, rtg.TC_BATCHED)[0] == 1
 
 
 def test_config2_holme_kim_full_size(ctx):
