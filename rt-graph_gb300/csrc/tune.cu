@@ -137,7 +137,7 @@ extern "C" rtg_status rtg_tune_tc(rtg_ctx *ctx, rtg_graph *g, const char *cache_
     }
     rtg_config best = def;
     double best_ms = def_ms;
-    for (uint32_t E : {128u, 256u, 512u})
+    for (uint32_t E : {128u, 256u, 512u, 1024u})
         for (uint32_t R : {512u, 1024u, 2048u})
             for (uint32_t W : {4u, 8u, 16u}) {
                 rtg_config c = def;
