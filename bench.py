@@ -121,8 +121,14 @@ class ClockSampler:
                 stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.t = threading.Thread(target=self._read, daemon=True)
             self.t.start()
+            # nvidia-smi takes ~0.1 s to print its first sample: wait for it (at most 5 s)
+            # so that the samples kept below fall inside the timed region
+            t_end = time.monotonic() + 5.0
+            while not self.lines and time.monotonic() < t_end and self.proc.poll() is None:
+                time.sleep(0.005)
         except (FileNotFoundError, OSError):
             self.proc = None
+        self.first = len(self.lines)
         return self
 
     def _read(self):
@@ -140,7 +146,9 @@ class ClockSampler:
     def summary(self) -> dict:
         sm, mx, reasons = [], None, set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        for line in self.lines:
+        # samples taken after the timed region began; all of them when it was too short
+        lines = self.lines[self.first:] or self.lines
+        for line in lines:
             p = [x.strip() for x in line.split(",")]
             if len(p) < 9:
                 continue
