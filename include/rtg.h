@@ -146,7 +146,8 @@ typedef struct rtg_graph_info {
  * any field means "library default". */
 typedef struct rtg_config {
     uint32_t tc_block_warps;    /* warps per block of the persistent TC kernel        */
-    uint32_t tc_item_edges;     /* in-edges of one vertex per work item               */
+    uint32_t tc_item_edges;     /* in-edges of one vertex per work item (default: 1024
+                                   from 2^23 oriented edges up, else 256)            */
     uint32_t tc_region_words;   /* 32-bit words of shared memory per warp for the
                                    out-list of the item's vertex: a bitmap of 32x that
                                    many ranks, or a hash table (power of two, 64..16384) */
