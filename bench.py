@@ -10,10 +10,15 @@ oriented by degree. A step is one exact uint64 count of the resident CSR:
   e2e     – the same metric through the public C ABI with host buffers:
             rtg_tc_count_host_edges (pinned host edges -> H2D -> GPU CSR build -> count ->
             D2H of the total), wall time per call.
-  plain   – the PLAIN form (one launch per bucket) on the same CSR, for the batched/plain
-            ratio.
-  roofline– the persistent kernel's algorithmic bytes (4 * sum over oriented edges of
-            (d+(u) + d+(v)) + 8 m) / its CUDA-event duration vs the measured HBM peak.
+  plain   – the PLAIN form (one launch per bucket, one warp per oriented edge, the
+            reference's per-edge formulation) on the same CSR, for the batched/plain ratio.
+  roofline– the persistent kernel's own algorithmic bytes per launch (4 B per streamed
+            suffix element, 8 B per in-edge range, 4 B per out-list element marked, 16 B of
+            offsets per vertex) over its CUDA-event duration against the measured HBM copy
+            peak; beside it the per-edge work formula of the measurement plan
+            (4 x sum over oriented edges of (d+(u) + d+(v)) + 8 m) as a work-equivalent
+            rate, and the DRAM traffic, issue activity and instructions per element from
+            the committed ncu summary of the same kernel.
   cpu_baseline – the oracle's restatement of the reference's ListIntersectionKernel
             (bs_tc.cu:120-148) on the host cores, on a stride sample of source vertices.
   si      – summary of the batched set-intersection workload (1e6 pairs of sorted unique
@@ -23,8 +28,11 @@ oriented by degree. A step is one exact uint64 count of the resident CSR:
             through rtg_si_count, and its roofline. `--workload si` prints that workload
             alone as a full line (with its CPU baseline).
 
-`--impl reference` runs only the reference's CPU algorithm (oracle port; the reference's
-own code cannot be built on the benchmark host) on the same workload and prints its line.
+`--impl reference` times the reference's counting logic on the host cores: the oracle's
+restatement of ListIntersectionKernel (the reference's own sources are not present on the
+benchmark host, and its GPU formulations need OptiX or are the same per-edge algorithm),
+on a stride sample of the same workload, which it generates with the oracle's copy of the
+seeded generator, so that the library under test is not loaded in that process.
 With torchrun (N>1) every rank runs an independent replica on its own GPU (the count does
 not shard across GPUs here); rank 0 prints one line with the max time over ranks.
 """
@@ -175,21 +183,57 @@ def measured_peaks() -> dict:
     return {"hbm_gbs": 6800.0, "source": "fallback"}
 
 
+def profile_fields(name: str) -> dict:
+    """Machine-readable `key: value` lines of a committed ncu summary (profiles/NAME.txt):
+    dram_bytes_per_full_launch, issue_active, warp_instructions, ..."""
+    p = REPO / "profiles" / f"{name}.txt"
+    out = {}
+    if not p.exists():
+        return out
+    for line in p.read_text().splitlines():
+        if ":" not in line or line.startswith(" "):
+            continue
+        k, v = line.split(":", 1)
+        try:
+            out[k.strip()] = float(v.split()[0])
+        except (ValueError, IndexError):
+            continue
+    return out
+
+
 def profile_traffic(name: str):
     """DRAM bytes per launch of the dominant kernel from a committed ncu summary."""
-    p = REPO / "profiles" / f"{name}.txt"
-    if not p.exists():
-        return None
-    for line in p.read_text().splitlines():
-        if line.startswith("dram_bytes_per_full_launch:"):
-            return int(float(line.split(":")[1]))
-    return None
+    v = profile_fields(name).get("dram_bytes_per_full_launch")
+    return int(v) if v else None
 
 
-def gen_workload():
-    import rtg
-    return rtg.gen_rmat(WORKLOAD["scale"], WORKLOAD["edge_factor"], *WORKLOAD["abcd"][:3],
-                        seed=WORKLOAD["seed"])
+def gen_workload(with_library: bool = True):
+    """The seeded R-MAT edge list: the library's generator, or the oracle's copy of the same
+    stream (identical arrays) for the reference arm, which does not load the library."""
+    if with_library:
+        import rtg
+        gen = rtg.gen_rmat
+    else:
+        import oracle
+        gen = oracle.gen_rmat
+    return gen(WORKLOAD["scale"], WORKLOAD["edge_factor"], *WORKLOAD["abcd"][:3],
+               seed=WORKLOAD["seed"])
+
+
+def tc_config(n: int, m: int, m_input: int, max_out: int) -> dict:
+    """The workload identity both arms report (same keys, same values)."""
+    return dict(WORKLOAD, n=int(n), m=int(m), m_input=int(m_input), max_out_degree=int(max_out))
+
+
+def tc_kernel_bytes(off: np.ndarray) -> tuple[int, int]:
+    """(streamed suffix elements, algorithmic bytes per launch) of the batched count:
+    every oriented edge u->v streams the suffix of N+(u) after v, sum over u of
+    d+(u)(d+(u)-1)/2 elements of 4 B; each in-edge range is 8 B; each out-list is marked
+    once (4 B per oriented edge); two u64 offsets per vertex."""
+    d = np.diff(off.astype(np.int64))
+    elems = int((d * (d - 1) // 2).sum())
+    n, m = len(d), int(d.sum())
+    return elems, 4 * elems + 12 * m + 16 * n
 
 
 def cpu_baseline_tc(off: np.ndarray, adj: np.ndarray, target_s: float = 15.0) -> dict:
@@ -215,11 +259,15 @@ def cpu_baseline_tc(off: np.ndarray, adj: np.ndarray, target_s: float = 15.0) ->
                       "ListIntersectionKernel restatement (per edge x binary search), OpenMP"}
 
 
-def gen_si_workload():
-    import rtg
-    return rtg.gen_si_pairs(SI_WORKLOAD["npairs"], median=64.0, sigma=1.5, min_len=1,
-                            max_len=65536, universe_log2=26, overlap_max=0.5,
-                            seed=SI_WORKLOAD["seed"])
+def gen_si_workload(with_library: bool = True):
+    if with_library:
+        import rtg
+        gen = rtg.gen_si_pairs
+    else:
+        import oracle
+        gen = oracle.gen_si_pairs
+    return gen(SI_WORKLOAD["npairs"], median=64.0, sigma=1.5, min_len=1, max_len=65536,
+               universe_log2=26, overlap_max=0.5, seed=SI_WORKLOAD["seed"])
 
 
 def dram_view(traffic, kernel_ms: float, peak_gbs: float, note: str) -> dict:
@@ -258,7 +306,7 @@ def run_reference_si(args, dist: Dist) -> None:
     if dist.rank != 0:
         return
     import oracle
-    off, el, pa, pb, exp = gen_si_workload()
+    off, el, pa, pb, exp = gen_si_workload(with_library=False)
     threads = os.cpu_count() or 1
     k = max(1, len(pa) // args.ref_stride)
     sel = np.arange(0, len(pa), len(pa) // k, dtype=np.int64)[:k]
@@ -534,7 +582,7 @@ def run_reference(args, dist: Dist) -> None:
     if dist.rank != 0:
         return
     import oracle
-    s, d = gen_workload()
+    s, d = gen_workload(with_library=False)
     off, adj = oracle.degree_csr(s, d)
     m = len(adj)
     off32, adj32 = off.astype(np.int32), adj.astype(np.int32)
@@ -552,15 +600,18 @@ def run_reference(args, dist: Dist) -> None:
         times.append(time.perf_counter() - t0)
     ms = 1e3 * sum(times) / len(times)
     value = sampled_edges / (ms / 1e3)
+    sample = (f"every {stride}-th source vertex of the oriented CSR ({sampled_edges} of {m} "
+              f"oriented edges per step, {ms / 1e3:.2f} s); restatement of the reference's "
+              "ListIntersectionKernel (tc/bs_tc/bs_tc.cu:120-148), per edge x binary search, "
+              f"OpenMP on {threads} threads; edges/s = sampled edges / step time")
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u32",
-            "data": "synthetic (seeded R-MAT)", "impl": "reference",
-            "config": dict(WORKLOAD, m=m, sample_stride=stride, sampled_edges=sampled_edges),
+            "data": "synthetic (seeded R-MAT, the oracle's copy of the generator)",
+            "impl": "reference",
+            "config": tc_config(n, m, len(s), int(np.diff(off).max()) if m else 0),
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
-                             "sample": f"every {stride}-th source vertex, {sampled_edges} "
-                                       "oriented edges per step; restatement of the reference's "
-                                       "ListIntersectionKernel (tc/bs_tc/bs_tc.cu:120-148)"},
+                             "sample": sample},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
@@ -625,19 +676,30 @@ def run_gpu(args, dist: Dist) -> None:
     e2e_value, _ = aggregate(dist, m, sum(e2e_ms) / len(e2e_ms))
     kms = sum(kms_steps) / len(kms_steps)
     peaks = measured_peaks()
-    achieved = algo_bytes / (kms / 1e3) / 1e9
+    off, adj = g.csr()
+    elems, kbytes = tc_kernel_bytes(off)
+    prof = profile_fields("tc_batched_rmat21")
+    achieved = kbytes / (kms / 1e3) / 1e9
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",
                 "frac": achieved / peaks["hbm_gbs"], "traffic": profile_traffic("tc_batched_rmat21"),
-                "peak_source": peaks["source"], "kernel": "k_tc_warp",
-                "kernel_ms": kms, "algo_bytes_per_launch": algo_bytes}
+                "peak_source": peaks["source"], "kernel": "k_tc_warp", "kernel_ms": kms,
+                "algo_bytes_per_launch": kbytes, "streamed_elements": elems,
+                "algo_bytes_basis": "4 B per streamed suffix element + 8 B per in-edge range + "
+                                    "4 B per out-list element + 16 B of offsets per vertex",
+                "work_equiv_bytes": algo_bytes,
+                "work_equiv_gbs": algo_bytes / (kms / 1e3) / 1e9,
+                "work_equiv_basis": "4 x sum over oriented edges of (d+(u) + d+(v)) + 8 m: both "
+                                    "full out-lists per edge, which this kernel never streams"}
+    if "issue_active" in prof:
+        roofline["issue_active"] = prof["issue_active"]
+    if "warp_instructions" in prof:
+        roofline["inst_per_elem"] = 32 * prof["warp_instructions"] / elems
+        roofline["inst_per_elem_basis"] = "32 x ncu warp instructions / streamed elements"
     roofline.update(dram_view(roofline["traffic"], kms, peaks["hbm_gbs"],
-                              "the formula charges both full out-lists of every oriented edge; "
-                              "the kernel streams only in-edge suffixes (2.98e9 elements) "
-                              "against shared-memory bitmaps: issue-bound (84 % issue-active "
-                              "by ncu), DRAM traffic below"))
+                              "most of the algorithmic bytes are served from L2; the limiter "
+                              "is instruction issue (issue_active), not DRAM (dram_frac)"))
     cpu = None
     if dist.rank == 0 and dist.ws == 1 and not args.no_cpu_baseline:
-        off, adj = g.csr()
         cpu = cpu_baseline_tc(off, adj)
     g.close()
     si = None
@@ -671,11 +733,11 @@ def run_gpu(args, dist: Dist) -> None:
                 "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
                 "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u32",
                 "data": "synthetic (seeded R-MAT, generated on the host)",
-                "config": dict(WORKLOAD, n=info.n, m=m, m_input=info.m_input,
-                               max_out_degree=info.max_out_degree, triangles=want,
-                               mode="batched", l2="flushed before every step",
-                               timing="CUDA events around each count on the context stream",
-                               parallelism="replicas" if dist.ws > 1 else "single GPU"),
+                "config": tc_config(info.n, m, info.m_input, info.max_out_degree),
+                "triangles": want,
+                "run": {"mode": "batched", "l2": "flushed before every step",
+                        "timing": "CUDA events around each count on the context stream",
+                        "parallelism": "replicas" if dist.ws > 1 else "single GPU"},
                 "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(te.h2d_bytes),
                         "d2h_bytes_per_step": int(te.d2h_bytes),
                         "ms_per_step": sum(e2e_ms) / len(e2e_ms),

@@ -28,7 +28,7 @@ def _load():
         import subprocess
         LIB_PATH.parent.mkdir(parents=True, exist_ok=True)
         subprocess.run(["gcc", "-O3", "-fPIC", "-shared", "-fopenmp", "-std=c11",
-                        str(HERE / "rtg_oracle.c"), "-o", str(LIB_PATH)], check=True)
+                        str(HERE / "rtg_oracle.c"), "-o", str(LIB_PATH), "-lm"], check=True)
     lib = C.CDLL(str(LIB_PATH))
     P = C.c_void_p
     sig = {
@@ -45,6 +45,12 @@ def _load():
         "orc_si_pairs": (None, [P, P, P, P, C.c_uint64, P, C.c_int]),
         "orc_si_dense": (None, [P, P, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32, P, C.c_int]),
         "orc_si_materialize": (C.c_uint64, [P, P, P, P, C.c_uint64, P, P, C.c_uint64]),
+        "orc_gen_rmat": (C.c_int, [C.c_uint32, C.c_uint32, C.c_double, C.c_double, C.c_double,
+                                   C.c_uint64, P, P, C.c_int]),
+        "orc_gen_si_lengths": (C.c_int, [C.c_uint64, C.c_double, C.c_double, C.c_uint32,
+                                         C.c_uint32, C.c_uint64, P, P, C.c_int]),
+        "orc_gen_si_lists": (C.c_int, [C.c_uint64, C.c_uint32, C.c_double, C.c_uint64, P, P, P,
+                                       P, C.c_int]),
     }
     for k, (r, a) in sig.items():
         f = getattr(lib, k)
@@ -163,3 +169,35 @@ def si_materialize(off, elems, pa, pb):
     el = np.zeros(max(need, 1), np.uint32)
     lib.orc_si_materialize(_p(off), _p(elems), _p(pa), _p(pb), len(pa), _p(oo), _p(el), need)
     return oo, el[:need]
+
+
+def gen_rmat(scale: int, edge_factor: int = 16, a=0.57, b=0.19, c=0.19, seed: int = 1,
+             threads: int = 0):
+    """Seeded R-MAT edge list (the same stream as the library's generator)."""
+    m = edge_factor << scale
+    s = np.empty(m, np.uint32)
+    d = np.empty(m, np.uint32)
+    if lib.orc_gen_rmat(scale, edge_factor, a, b, c, seed, _p(s), _p(d), threads) != 0:
+        raise ValueError("bad R-MAT parameters")
+    return s, d
+
+
+def gen_si_pairs(npairs: int, median=64.0, sigma=1.5, min_len=1, max_len=65536,
+                 universe_log2=26, overlap_max=0.5, seed: int = 1, threads: int = 0):
+    """Seeded batched-SI workload (the same streams as the library's generator): set
+    offsets, elements, pair ids (2i, 2i + 1) and the known overlap of every pair."""
+    if 2 * max_len > (1 << universe_log2):
+        raise ValueError("max_len too large for the universe")
+    lens = np.empty(2 * npairs, np.uint32)
+    tot = C.c_uint64(0)
+    if lib.orc_gen_si_lengths(npairs, median, sigma, min_len, max_len, seed, _p(lens),
+                              C.byref(tot), threads) != 0:
+        raise ValueError("bad SI parameters")
+    off = np.empty(2 * npairs + 1, np.uint64)
+    el = np.empty(tot.value, np.uint32)
+    exp = np.empty(npairs, np.uint32)
+    if lib.orc_gen_si_lists(npairs, universe_log2, overlap_max, seed, _p(lens), _p(off), _p(el),
+                            _p(exp), threads) != 0:
+        raise MemoryError("SI generator")
+    pa = np.arange(0, 2 * npairs, 2, dtype=np.uint32)
+    return off, el, pa, pa + 1, exp

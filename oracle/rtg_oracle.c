@@ -4,6 +4,7 @@
  */
 #include "rtg_oracle.h"
 
+#include <math.h>
 #include <omp.h>
 #include <stdlib.h>
 #include <string.h>
@@ -392,4 +393,211 @@ uint64_t orc_si_materialize(const uint64_t *off, const uint32_t *elems, const ui
     }
     out_off[np] = w;
     return w;
+}
+
+/* ------------------------------------------------------------------ workload generators
+ * Seeded synthetic inputs for the timed CPU reference arm, so that it generates its
+ * workload without the library under test. Same streams as the library's generators
+ * (rt-graph_gb300/csrc/gen.cpp); the tests check that both give identical arrays. */
+
+static inline uint64_t orc_splitmix64(uint64_t *x) {
+    uint64_t z = (*x += 0x9E3779B97F4A7C15ull);
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
+}
+
+static inline uint64_t orc_hash3(uint64_t seed, uint64_t a, uint64_t b) {
+    uint64_t x = seed ^ (a * 0xD6E8FEB86659FD93ull) ^ (b * 0xA0761D6478BD642Full);
+    return orc_splitmix64(&x);
+}
+
+static uint32_t orc_threshold32(double p) {
+    if (p <= 0) return 0;
+    if (p >= 1) return 0xFFFFFFFFu;
+    return (uint32_t)floor(p * 4294967296.0);
+}
+
+int orc_gen_rmat(uint32_t scale, uint32_t edge_factor, double a, double b, double c,
+                 uint64_t seed, uint32_t *src, uint32_t *dst, int threads) {
+    if (!src || !dst || scale == 0 || scale > 31 || edge_factor == 0) return -1;
+    set_threads(threads);
+    const uint64_t m = (uint64_t)edge_factor << scale;
+    const uint32_t ta = orc_threshold32(a), tb = orc_threshold32(a + b),
+                   tc = orc_threshold32(a + b + c);
+#pragma omp parallel for schedule(static)
+    for (int64_t i = 0; i < (int64_t)m; ++i) {
+        uint32_t s = 0, d = 0;
+        uint64_t r = 0;
+        for (uint32_t l = 0; l < scale; ++l) {
+            /* one 64-bit draw per two levels: low half for even levels, high half for odd */
+            if ((l & 1) == 0) r = orc_hash3(seed, (uint64_t)i, l >> 1);
+            const uint32_t u = (uint32_t)(r >> ((l & 1) ? 32 : 0));
+            const uint32_t sb = u >= tb, db = (u >= ta && u < tb) || u >= tc;
+            s = (s << 1) | sb;
+            d = (d << 1) | db;
+        }
+        src[i] = s;
+        dst[i] = d;
+    }
+    return 0;
+}
+
+/* xoshiro256** seeded by splitmix64, and Lemire's unbiased bounded draw (as in gen.cpp) */
+typedef struct {
+    uint64_t s[4];
+} orc_xoshiro;
+
+static void orc_xo_seed(orc_xoshiro *g, uint64_t seed) {
+    uint64_t x = seed;
+    for (int k = 0; k < 4; ++k) g->s[k] = orc_splitmix64(&x);
+}
+
+static inline uint64_t orc_rotl(uint64_t x, int k) { return (x << k) | (x >> (64 - k)); }
+
+static inline uint64_t orc_xo_next(orc_xoshiro *g) {
+    uint64_t *s = g->s;
+    const uint64_t r = orc_rotl(s[1] * 5, 7) * 9;
+    const uint64_t t = s[1] << 17;
+    s[2] ^= s[0];
+    s[3] ^= s[1];
+    s[1] ^= s[2];
+    s[0] ^= s[3];
+    s[2] ^= t;
+    s[3] = orc_rotl(s[3], 45);
+    return r;
+}
+
+static inline uint64_t orc_xo_below(orc_xoshiro *g, uint64_t n) {
+    unsigned __int128 m = (unsigned __int128)orc_xo_next(g) * n;
+    uint64_t l = (uint64_t)m;
+    if (l < n) {
+        const uint64_t t = (0 - n) % n;
+        while (l < t) {
+            m = (unsigned __int128)orc_xo_next(g) * n;
+            l = (uint64_t)m;
+        }
+    }
+    return (uint64_t)(m >> 64);
+}
+
+static int orc_cmp_u32(const void *a, const void *b) {
+    const uint32_t x = *(const uint32_t *)a, y = *(const uint32_t *)b;
+    return (x > y) - (x < y);
+}
+
+/* sort ascending and drop repeats; returns the new length */
+static size_t orc_sort_unique(uint32_t *v, size_t n) {
+    if (n < 2) return n;
+    qsort(v, n, 4, orc_cmp_u32);
+    size_t w = 1;
+    for (size_t i = 1; i < n; ++i)
+        if (v[i] != v[w - 1]) v[w++] = v[i];
+    return w;
+}
+
+static int orc_contains(const uint32_t *v, uint32_t n, uint32_t x) {
+    uint32_t lo = 0, hi = n;
+    while (lo < hi) {
+        const uint32_t mid = lo + (hi - lo) / 2;
+        if (v[mid] < x) lo = mid + 1;
+        else hi = mid;
+    }
+    return lo < n && v[lo] == x;
+}
+
+int orc_gen_si_lengths(uint64_t npairs, double median, double sigma, uint32_t min_len,
+                       uint32_t max_len, uint64_t seed, uint32_t *len, uint64_t *total,
+                       int threads) {
+    if (!len || !total || median <= 0 || sigma < 0 || min_len == 0 || max_len < min_len)
+        return -1;
+    set_threads(threads);
+    const double mu = log(median);
+    uint64_t tot = 0;
+#pragma omp parallel for reduction(+ : tot) schedule(static)
+    for (int64_t i = 0; i < (int64_t)(2 * npairs); ++i) {
+        /* lognormal length by Box-Muller on two hashed uniforms, floored and clamped */
+        const uint64_t r = orc_hash3(seed, 0x5151u, (uint64_t)i);
+        const double u1 = ((double)(r >> 11) + 0.5) * 0x1.0p-53;
+        const uint64_t r2 = orc_hash3(seed, 0x5152u, (uint64_t)i);
+        const double u2 = (double)(r2 >> 11) * 0x1.0p-53;
+        const double z = sqrt(-2.0 * log(u1)) * cos(6.283185307179586 * u2);
+        const double x = floor(exp(mu + sigma * z));
+        const uint32_t l =
+            (x < (double)min_len) ? min_len : (x > (double)max_len ? max_len : (uint32_t)x);
+        len[i] = l;
+        tot += l;
+    }
+    *total = tot;
+    return 0;
+}
+
+int orc_gen_si_lists(uint64_t npairs, uint32_t universe_log2, double overlap_max, uint64_t seed,
+                     const uint32_t *len, uint64_t *offsets, uint32_t *elems, uint32_t *expected,
+                     int threads) {
+    if (!len || !offsets || !elems || !expected || universe_log2 == 0 || universe_log2 > 31)
+        return -1;
+    set_threads(threads);
+    const uint64_t U = 1ull << universe_log2;
+    offsets[0] = 0;
+    uint32_t maxl = 0;
+    for (uint64_t i = 0; i < 2 * npairs; ++i) {
+        offsets[i + 1] = offsets[i] + len[i];
+        if (len[i] > maxl) maxl = len[i];
+    }
+    int bad = 0;
+#pragma omp parallel
+    {
+        uint32_t *buf = (uint32_t *)malloc(sizeof(uint32_t) * (maxl ? 2 * (size_t)maxl : 1));
+        uint32_t *idx = (uint32_t *)malloc(sizeof(uint32_t) * (maxl ? maxl : 1));
+        if (!buf || !idx) {
+#pragma omp atomic write
+            bad = 1;
+        }
+#pragma omp for schedule(dynamic, 64)
+        for (int64_t i = 0; i < (int64_t)npairs; ++i) {
+            if (!buf || !idx) continue;
+            orc_xoshiro g;
+            orc_xo_seed(&g, orc_hash3(seed, 0x5153u, (uint64_t)i));
+            const uint64_t sa = 2 * (uint64_t)i, sb = sa + 1;
+            const int a_long = len[sa] >= len[sb];
+            const uint64_t sl = a_long ? sa : sb, ss = a_long ? sb : sa;
+            const uint32_t L = len[sl], S = len[ss];
+            uint32_t *Lp = elems + offsets[sl], *Sp = elems + offsets[ss];
+            /* long list: L distinct uniform values, topped up after each sort + unique */
+            size_t nb = 0;
+            while (nb < L) {
+                const size_t need = L - nb;
+                for (size_t k = 0; k < need; ++k) buf[nb++] = (uint32_t)orc_xo_below(&g, U);
+                nb = orc_sort_unique(buf, nb);
+            }
+            memcpy(Lp, buf, (size_t)L * 4);
+            /* short list: k elements of the long list (partial Fisher-Yates), the rest
+             * distinct values outside it */
+            const double f = (double)(orc_xo_next(&g) >> 11) * 0x1.0p-53 * overlap_max;
+            const uint32_t k = (uint32_t)floor(f * S);
+            for (uint32_t t = 0; t < L; ++t) idx[t] = t;
+            nb = 0;
+            for (uint32_t t = 0; t < k; ++t) {
+                const uint32_t r = t + (uint32_t)orc_xo_below(&g, L - t);
+                const uint32_t tmp = idx[t];
+                idx[t] = idx[r];
+                idx[r] = tmp;
+                buf[nb++] = Lp[idx[t]];
+            }
+            while (nb < S) {
+                const size_t need = S - nb;
+                for (size_t q = 0; q < need; ++q) {
+                    const uint32_t x = (uint32_t)orc_xo_below(&g, U);
+                    if (!orc_contains(Lp, L, x)) buf[nb++] = x;
+                }
+                nb = orc_sort_unique(buf, nb);
+            }
+            memcpy(Sp, buf, (size_t)S * 4);
+            expected[i] = k;
+        }
+        free(buf);
+        free(idx);
+    }
+    return bad ? -1 : 0;
 }

@@ -153,7 +153,7 @@ def build_oracle() -> Path | None:
     out.parent.mkdir(parents=True, exist_ok=True)
     if _stale(out, [src, ORACLE / "rtg_oracle.h"]):
         _run([CC, "-O3", "-fPIC", "-shared", "-fopenmp", "-std=c11", "-Wall",
-              str(src), "-o", str(out)])
+              str(src), "-o", str(out), "-lm"])
     return out
 
 

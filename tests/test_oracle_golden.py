@@ -114,3 +114,23 @@ def test_tc_oracle_closed_forms():
     d = (s - 1) // 2
     off, adj = oracle.degree_csr(s, d.astype(np.uint32))
     assert oracle.tc_merge(off, adj) == 0
+
+
+@pytest.mark.parametrize("scale,seed", [(8, 1), (12, 42), (14, 7)])
+def test_oracle_rmat_generator_matches_library(scale, seed):
+    """The reference arm of the benchmark makes its R-MAT input with the oracle's
+    generator: it must give the library generator's edge list, bit for bit."""
+    import rtg
+    s0, d0 = rtg.gen_rmat(scale, 16, 0.57, 0.19, 0.19, seed=seed)
+    s1, d1 = oracle.gen_rmat(scale, 16, 0.57, 0.19, 0.19, seed=seed)
+    assert np.array_equal(s0, s1) and np.array_equal(d0, d1)
+
+
+def test_oracle_si_generator_matches_library():
+    import rtg
+    a = rtg.gen_si_pairs(3000, seed=11)
+    b = oracle.gen_si_pairs(3000, seed=11)
+    for x, y in zip(a, b):
+        assert np.array_equal(x, y)
+    off, el, pa, pb, exp = b
+    assert np.array_equal(oracle.si_pairs(off, el, pa, pb), exp)
