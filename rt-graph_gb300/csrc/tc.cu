@@ -13,17 +13,19 @@
 //           suffix of N+(u) after v can meet N+(v), so each in-edge is a ready-made element
 //           range. A work item is (v, first in-edge): up to E in-edges of one vertex v, taken
 //           by one warp from a device queue (persistent kernel, no block barriers). The warp
-//           marks N+(v) in its shared-memory region: as a bitmap over the ranks [b0, n), b0 =
-//           v + 1 rounded down to a multiple of 32, when n - b0 fits the region (high-rank v,
-//           which carry almost all of the work on power-law graphs), else as an open-addressing
-//           hash table, else (out-list too long for the table) it falls back to a tile merge. It then streams the suffixes of the
-//           item's in-edges as 64-element blocks (two coalesced loads per lane), three
-//           blocks in flight ahead of the one being tested, and tests every element with one
-//           shared-memory load.
+//           marks N+(v) in its shared-memory region: a bitmap over the top ranks of the graph
+//           (from v + 1 when they fit, which holds for the high-rank v that carry almost all
+//           of the work on power-law graphs), plus a small hash table for the few elements
+//           of N+(v) below that window; out-lists with too many such elements fall back to
+//           a tile merge. It then streams the suffixes of the item's in-edges 32 at a time:
+//           whole 64-element units of each suffix with unchecked coalesced loads, then the
+//           remainders of all 32 suffixes as one flat sequence in full 32-lane windows,
+//           testing every element with one shared-memory load.
 //           Streamed elements: sum over u of d+(u)(d+(u)-1)/2, about a quarter of the
-//           push-order work on power-law graphs. Item build + count are one CUDA graph,
-//           captured once per (graph, schedule) and replayed. uint64 totals: lane partials ->
-//           warp shuffle sum -> block sum -> one atomicAdd per block.
+//           push-order work on power-law graphs. The items are built once per (graph,
+//           schedule); the count (counter resets + the persistent kernel) is one CUDA graph,
+//           captured once and replayed. uint64 totals: lane partials -> warp shuffle sum ->
+//           block sum -> one atomicAdd per block.
 #include <cub/cub.cuh>
 
 #include <algorithm>
@@ -188,151 +190,166 @@ struct WarpCfg {
     uint32_t n;      // vertices of the counting form
 };
 
-// Stream the suffix ranges of the item's in-edges [k0, k1) (edge k's range is in_rng[kin+k])
-// as a sequence of blocks of 32 * kLoads elements, kLoads coalesced 32-bit loads per lane
-// per block (elements X + lane + 32 j); a block never spans two suffixes. Two loads per
-// block halve the per-block bookkeeping against one, at 73 % full blocks instead of 86 % on
-// R-MAT-21's suffixes. kDepth blocks are in flight ahead of the block being tested, and the
-// pipeline runs across edge and batch boundaries; the ranges of the next 32 in-edges are
-// loaded one batch ahead. Elements past the end of a suffix read as `idle`, and f(idle)
-// must be 0. f(w) tests one element. The per-lane count of one item fits 32 bits (at most
-// E in-edges of at most n elements each / 32).
-constexpr int kLoads = 2;
-constexpr int kDepth = 3;
+// 1 << s for s < 32, 0 for s >= 32 (PTX clamps the shift amount; C++ leaves it undefined)
+__device__ __forceinline__ uint32_t bit_or_zero(uint32_t s) {
+    uint32_t r;
+    asm("shl.b32 %0, 1, %1;" : "=r"(r) : "r"(s));
+    return r;
+}
+
+// Stream the suffix ranges of the item's in-edges [k0, k1) (edge k's range is in_rng[k]),
+// 32 in-edges at a time (lane k holds in-edge kb + k; the next batch's ranges are loaded
+// one batch ahead), and test every element with f (f(idle) must be 0). Per batch:
+//  1. units: every whole 64-element unit of every suffix, two coalesced 32-bit loads per
+//     lane and no bounds check; the warp visits only the in-edges that have units (a
+//     ballot mask), and the next unit's loads are issued before the current one is tested;
+//  2. remainders: the last (length mod 64) elements of all 32 suffixes, concatenated into
+//     one sequence (in-edges with an empty remainder compacted out through `cmp`, 32
+//     entries of per-warp shared memory) and swept in 32-position windows with every lane
+//     busy: the in-edges that start inside a window are one OR-reduction of a bit per
+//     in-edge, and lane L finds its in-edge by counting the starts at or before it.
+// The per-lane count of one item fits 32 bits (at most E in-edges of at most n elements).
+constexpr uint32_t kUnit = 64;
+constexpr int kUnitDepth = 3;  // units whose loads are in flight ahead of the one tested
+constexpr int kWin = 4;        // remainder windows whose loads are in flight together
 
 template <class F>
 __device__ __forceinline__ uint32_t stream_item(const uint32_t *__restrict__ adj,
                                                 const uint2 *__restrict__ rng, uint32_t k0,
-                                                uint32_t k1, int lane, uint32_t idle, F f) {
+                                                uint32_t k1, int lane, uint32_t idle,
+                                                uint2 *cmp, F f) {
     uint32_t cnt = 0;
-    uint32_t kb = k0;
-    uint32_t nb = min(32u, k1 - kb);
-    uint2 my = (kb + lane < k1) ? __ldg(rng + kb + lane) : make_uint2(0u, 0u);
-    uint2 nx = (kb + 32 + lane < k1) ? __ldg(rng + kb + 32 + lane) : make_uint2(0u, 0u);
-    uint32_t e = 0;
-    uint32_t X = __shfl_sync(kFull, my.x, 0), Y = __shfl_sync(kFull, my.y, 0);
-    bool live = true;
-    // move (e, X, Y) to the next edge with elements left; warp-uniform. When the item is
-    // exhausted it stops with X >= Y, so every later block is all idle without a check.
-    auto settle = [&]() {
-        while (live && X >= Y) {
-            if (++e >= nb) {
-                kb += 32;
-                if (kb >= k1) {
-                    live = false;
-                    break;
-                }
-                nb = min(32u, k1 - kb);
-                my = nx;
-                nx = (kb + 32 + lane < k1) ? __ldg(rng + kb + 32 + lane) : make_uint2(0u, 0u);
-                e = 0;
-            }
-            X = __shfl_sync(kFull, my.x, e);
-            Y = __shfl_sync(kFull, my.y, e);
-        }
-    };
-    struct Block {
-        uint32_t w[kLoads];
-    };
-    auto next_block = [&]() -> Block {
-        const uint32_t i = X + lane;
-        Block b;
-#pragma unroll
-        for (int j = 0; j < kLoads; ++j) b.w[j] = i + 32 * j < Y ? __ldg(adj + i + 32 * j) : idle;
-        X += 32 * kLoads;
-        if (__builtin_expect(X >= Y, 0)) settle();  // once per in-edge: keep it off the block path
-        return b;
-    };
-    settle();
-    Block buf[kDepth];
-#pragma unroll
-    for (int d = 0; d < kDepth; ++d) buf[d] = next_block();
-    while (live) {
-#pragma unroll
-        for (int d = 0; d < kDepth; ++d) {
-#pragma unroll
-            for (int j = 0; j < kLoads; ++j) cnt += f(buf[d].w[j]);
-            buf[d] = next_block();
-        }
-    }
-#pragma unroll
-    for (int d = 0; d < kDepth; ++d)
-#pragma unroll
-        for (int j = 0; j < kLoads; ++j) cnt += f(buf[d].w[j]);
-    return cnt;
-}
-
-// The same item as one flat sequence, for short suffixes: the suffix lengths of 32 in-edges
-// are scanned across the lanes, and each 32-position window of their concatenation is
-// spread over the lanes, so a block is full even when every suffix holds a few elements.
-// Each lane keeps a cursor on the in-edge holding its position (positions only grow, so the
-// cursor only moves forward, one shuffle pair per step, all lanes stepping together while
-// any lane needs to). kFlatWin windows' loads are in flight together.
-constexpr int kFlatWin = 4;
-
-template <class F>
-__device__ __forceinline__ uint32_t stream_item_flat(const uint32_t *__restrict__ adj,
-                                                     const uint2 *__restrict__ rng, uint32_t k0,
-                                                     uint32_t k1, int lane, F f) {
-    uint32_t cnt = 0;
+    const uint32_t le = 0xFFFFFFFFu >> (31 - lane);  // lanes 0..lane
+    const uint32_t lt = (1u << lane) - 1u;           // lanes below this one
+    const uint32_t *adjl = adj + lane;
     uint2 nx = (k0 + lane < k1) ? __ldg(rng + k0 + lane) : make_uint2(0u, 0u);
     for (uint32_t kb = k0; kb < k1; kb += 32) {
-        const uint2 my = nx;
+        const uint2 r = nx;
         nx = (kb + 32 + lane < k1) ? __ldg(rng + kb + 32 + lane) : make_uint2(0u, 0u);
-        const uint32_t len = my.y - my.x;  // lanes past the item hold (0, 0)
-        uint32_t inc = len;
+        const uint32_t len = r.y - r.x;  // 0 past the item
+        // ---- 1. whole units
+        const uint32_t nu = len / kUnit;
+        unsigned F = __ballot_sync(kFull, nu != 0);
+        if (F) {
+            uint32_t X = 0, left = 0;
+            // next unit's first element (warp-uniform); false when the batch has none left
+            auto next_unit = [&](uint32_t &ux) -> bool {
+                if (left == 0) {
+                    if (!F) return false;
+                    const int e = __ffs(F) - 1;
+                    F &= F - 1;
+                    X = __shfl_sync(kFull, r.x, e);
+                    left = __shfl_sync(kFull, nu, e);
+                }
+                ux = X;
+                X += kUnit;
+                --left;
+                return true;
+            };
+            // kUnitDepth units in flight; a unit past the last holds idle elements
+            uint32_t a[kUnitDepth][2];
+            bool live = true;
+            auto load_unit = [&](uint32_t *u) {
+                uint32_t ux = 0;
+                if (live && next_unit(ux)) {
+                    u[0] = __ldg(adjl + ux);
+                    u[1] = __ldg(adjl + ux + 32);
+                } else {
+                    live = false;
+                    u[0] = u[1] = idle;
+                }
+            };
+#pragma unroll
+            for (int d = 0; d < kUnitDepth; ++d) load_unit(a[d]);
+            while (live) {
+#pragma unroll
+                for (int d = 0; d < kUnitDepth; ++d) {
+                    cnt += f(a[d][0]) + f(a[d][1]);
+                    load_unit(a[d]);
+                }
+            }
+#pragma unroll
+            for (int d = 0; d < kUnitDepth; ++d) cnt += f(a[d][0]) + f(a[d][1]);
+        }
+        // ---- 2. remainders, one flat sequence
+        const uint32_t rl = len % kUnit;
+        const unsigned Z = __ballot_sync(kFull, rl != 0);
+        if (!Z) continue;
+        if (rl) cmp[__popc(Z & lt)] = make_uint2(r.x + (len - rl), rl);
+        __syncwarp();
+        const uint32_t nz = __popc(Z);
+        const uint2 c = (uint32_t)lane < nz ? cmp[lane] : make_uint2(0u, 0u);
+        __syncwarp();
+        uint32_t inc = c.y;
 #pragma unroll
         for (int o = 1; o < 32; o <<= 1) {
             const uint32_t t = __shfl_up_sync(kFull, inc, o);
             if (lane >= o) inc += t;
         }
         const uint32_t T = __shfl_sync(kFull, inc, 31);
-        const uint32_t ex = inc - len;    // first position of this lane's suffix
-        const uint32_t dx = my.x - ex;    // adj index of position p of this suffix: p + dx
-        const uint32_t nxs = __shfl_down_sync(kFull, ex, 1);
-        const uint32_t nstart = lane == 31 ? kEmpty : nxs;  // start of the next suffix
-        // per-lane cursor: the in-edge holding this lane's position (positions only grow)
-        uint32_t e = 0, d = __shfl_sync(kFull, dx, 0), ns = __shfl_sync(kFull, nstart, 0);
-        for (uint32_t t0 = 0; t0 < T; t0 += 32 * kFlatWin) {
-            uint32_t w[kFlatWin];
+        const uint32_t P = inc - c.y;     // first position of this lane's remainder
+        const uint32_t delta = c.x - P;   // adj index of position q of it: q + delta
+        // start of this lane's remainder relative to the window; lanes without one never
+        // start inside a window
+        uint32_t dP = (uint32_t)lane < nz ? P : 0x80000000u;
+        uint32_t before = 0;  // remainders starting before the window
+        for (uint32_t t0 = 0; t0 < T; t0 += 32 * kWin) {
+            uint32_t w[kWin];
 #pragma unroll
-            for (int j = 0; j < kFlatWin; ++j) {
-                const uint32_t pos = t0 + 32u * j + (uint32_t)lane;
-                while (__any_sync(kFull, pos >= ns && pos < T)) {
-                    const bool adv = pos >= ns && pos < T;
-                    const uint32_t e2 = e + 1;
-                    const uint32_t d2 = __shfl_sync(kFull, dx, e2 & 31);
-                    const uint32_t n2 = __shfl_sync(kFull, nstart, e2 & 31);
-                    if (adv) {
-                        e = e2;
-                        d = d2;
-                        ns = n2;
-                    }
-                }
-                w[j] = pos < T ? __ldg(adj + pos + d) : kEmpty;
+            for (int j = 0; j < kWin; ++j) {
+                const uint32_t M = __reduce_or_sync(kFull, bit_or_zero(dP));
+                const uint32_t eL = before + __popc(M & le) - 1;
+                const uint32_t dl = __shfl_sync(kFull, delta, eL & 31);
+                const uint32_t q = t0 + 32 * j + lane;
+                w[j] = q < T ? __ldg(adj + (q + dl)) : idle;
+                before += __popc(M);
+                dP -= 32;
             }
 #pragma unroll
-            for (int j = 0; j < kFlatWin; ++j)
-                if (t0 + 32u * j + (uint32_t)lane < T) cnt += f(w[j]);
+            for (int j = 0; j < kWin; ++j) cnt += f(w[j]);
         }
     }
     return cnt;
 }
 
+// Words of the per-warp hash table that holds the part of N+(v) below the bitmap window
+// when v sits too low for the window to reach it (at most kLowHashWords / 2 elements).
+constexpr uint32_t kLowHashWords = 128;
+constexpr uint32_t kLowHashLg = 7;
+// Per-warp region: R bitmap words, the guard word and one pad word (keeps what follows
+// 8-byte aligned; R is a power of two), the low-part hash table, and 32 uint2 entries of
+// scratch for compacting the remainders of a batch of in-edges.
+constexpr uint32_t kCmpWords = 64;
+__host__ __device__ constexpr uint32_t region_words(uint32_t R) {
+    return R + 2 + kLowHashWords + kCmpWords;
+}
+
 // acc[0] = total, acc[1] = item queue head, acc[2] = number of items
-__global__ void k_tc_warp(const uint64_t *__restrict__ off, const uint32_t *__restrict__ adj,
+//
+// Per item the warp marks N+(v) in its shared-memory region: a bitmap of R words over the
+// ranks [W0, n) (W0 a multiple of 32), with W0 = v + 1 rounded down when n - W0 fits the
+// bitmap (high-rank v: every element of N+(v) and of the suffixes is in the window), else
+// W0 = the lowest multiple of 32 with n - W0 <= 32 R, and the few elements of N+(v) below
+// W0 go to an open-addressing hash table of kLowHashWords words (0 marks an empty slot:
+// every element is a rank above v >= 0). A suffix element w is tested in the bitmap when
+// w >= W0, else in the table. An out-list with more than kLowHashWords / 2 elements below
+// the window (none on R-MAT or Holme-Kim graphs) is merged against each suffix instead.
+__global__ void __maxnreg__(48) k_tc_warp(const uint64_t *__restrict__ off, const uint32_t *__restrict__ adj,
                           const uint64_t *__restrict__ in_off, const uint2 *__restrict__ in_rng,
                           const uint64_t *__restrict__ items, unsigned long long *acc,
                           WarpCfg p) {
     extern __shared__ __align__(16) uint32_t smem[];
     __shared__ unsigned long long red[32];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    // R words of region + one guard word (reg[R]) that stays zero: idle lanes of the bitmap
-    // test read it instead of branching
-    uint32_t *reg = smem + (size_t)warp * (p.R + 1);
-    for (uint32_t q = lane; q <= p.R; q += 32) reg[q] = 0u;  // all-zero between items
+    // R words of bitmap + one guard word (reg[R]) that stays zero (idle lanes of the test
+    // read it instead of branching) + the low-part hash table + remainder scratch
+    uint32_t *reg = smem + (size_t)warp * region_words(p.R);
+    uint32_t *tab = reg + p.R + 2;
+    uint2 *cmp = reinterpret_cast<uint2 *>(tab + kLowHashWords);
+    for (uint32_t q = lane; q < p.R + 2 + kLowHashWords; q += 32) reg[q] = 0u;  // zero between items
     __syncwarp();
     const uint32_t RB = p.R * 32;  // bitmap capacity in bits
+    const uint32_t Wlow = p.n > RB ? ((p.n - RB + 31) & ~31u) : 0u;
     const unsigned long long nitems = acc[2];
     unsigned long long cnt = 0;
     while (true) {
@@ -347,44 +364,44 @@ __global__ void k_tc_warp(const uint64_t *__restrict__ off, const uint32_t *__re
         const uint64_t kin = in_off[v];
         const uint32_t k1 = min(k0 + p.E, (uint32_t)(in_off[v + 1] - kin));
         const uint32_t *Nv = adj + ov;
-        const uint32_t base0 = (v + 1) & ~31u;  // bitmap origin, a multiple of 32
-        const int mode = (p.n - base0 <= RB) ? 0 : (2 * b <= p.R ? 1 : 2);  // bitmap / hash / merge
-        uint32_t lg = 0;
-        if (mode == 0) {
-            for (uint32_t q = lane; q < b; q += 32) {
-                const uint32_t o = __ldg(Nv + q) - base0;
-                atomicOr(&reg[o >> 5], 1u << (o & 31));
-            }
-        } else if (mode == 1) {
-            // open addressing over the whole region (R slots, load b/R <= 1/2, mostly far
-            // less, so probes rarely go past the first slot); 0 marks an empty slot: every
-            // element of N+(v) is a rank above v, never 0, and the region is all-zero
-            lg = 31 - __clz(p.R);
-            const uint32_t mask = p.R - 1;
+        const uint32_t base0 = (v + 1) & ~31u;
+        // 0: bitmap only; 1: bitmap + low-part table; 2: merge
+        int mode = 0;
+        uint32_t W0 = base0;
+        if (p.n - base0 > RB) {
+            W0 = Wlow;
+            mode = (b > kLowHashWords / 2 && __ldg(Nv + kLowHashWords / 2) < W0) ? 2 : 1;
+        }
+        if (mode != 2) {
             for (uint32_t q = lane; q < b; q += 32) {
                 const uint32_t w = __ldg(Nv + q);
-                uint32_t sl = hash_slot(w, lg);
-                while (atomicCAS(&reg[sl], 0u, w) != 0u) sl = (sl + 1) & mask;
+                if (w >= W0) {
+                    const uint32_t o = w - W0;
+                    atomicOr(&reg[o >> 5], 1u << (o & 31));
+                } else {
+                    uint32_t sl = hash_slot(w, kLowHashLg);
+                    while (atomicCAS(&tab[sl], 0u, w) != 0u) sl = (sl + 1) & (kLowHashWords - 1);
+                }
             }
         }
         __syncwarp();
+        // bit w - W0 of the bitmap: word (w >> 5) - (W0 >> 5), bit w & 31 (W0 is a multiple
+        // of 32); idle lanes read the guard word reg[R]
+        const uint32_t *regp = reg - (W0 >> 5);
+        const uint32_t idle = W0 + RB;
         if (mode == 0) {
-            // bit w - base0 of the bitmap: word (w >> 5) - (base0 >> 5), bit w & 31 (base0 is
-            // a multiple of 32); idle lanes read the guard word reg[R]
-            const uint32_t *regp = reg - (base0 >> 5);
-            cnt += stream_item(adj, in_rng + kin, k0, k1, lane, base0 + 32 * p.R,
+            cnt += stream_item(adj, in_rng + kin, k0, k1, lane, idle, cmp,
                                [&](uint32_t w) -> uint32_t {
                                    return __funnelshift_r(regp[w >> 5], 0u, w) & 1u;
                                });
         } else if (mode == 1) {
-            // low-rank vertices: short out-lists and short suffixes, streamed flat
-            const uint32_t mask = p.R - 1;
-            cnt += stream_item_flat(adj, in_rng + kin, k0, k1, lane, [&](uint32_t w) -> uint32_t {
-                uint32_t sl = hash_slot(w, lg);
-                uint32_t x = reg[sl];
-                while (__builtin_expect(x != w && x != 0u, 0)) {
-                    sl = (sl + 1) & mask;
-                    x = reg[sl];
+            cnt += stream_item(adj, in_rng + kin, k0, k1, lane, idle, cmp, [&](uint32_t w) -> uint32_t {
+                if (w >= W0) return __funnelshift_r(regp[w >> 5], 0u, w) & 1u;
+                uint32_t sl = hash_slot(w, kLowHashLg);
+                uint32_t x = tab[sl];
+                while (x != w && x != 0u) {
+                    sl = (sl + 1) & (kLowHashWords - 1);
+                    x = tab[sl];
                 }
                 return x == w ? 1u : 0u;
             });
@@ -396,18 +413,13 @@ __global__ void k_tc_warp(const uint64_t *__restrict__ off, const uint32_t *__re
         }
         __syncwarp();
         // return the region to all-zero
-        if (mode == 0) {
-            for (uint32_t q = lane; q < b; q += 32) reg[(__ldg(Nv + q) - base0) >> 5] = 0u;
-        } else if (mode == 1) {
-            // zero the b occupied slots (each lane finds its elements again; a slot zeroed
-            // by another lane never ends a search, which stops only on its own element)
-            const uint32_t mask = p.R - 1;
+        if (mode != 2) {
             for (uint32_t q = lane; q < b; q += 32) {
                 const uint32_t w = __ldg(Nv + q);
-                uint32_t sl = hash_slot(w, lg);
-                while (reg[sl] != w) sl = (sl + 1) & mask;
-                reg[sl] = 0u;
+                if (w >= W0) reg[(w - W0) >> 5] = 0u;
             }
+            if (mode == 1)
+                for (uint32_t q = lane; q < kLowHashWords; q += 32) tab[q] = 0u;
         }
         __syncwarp();
     }
@@ -488,7 +500,7 @@ rtg_status batched_shape(rtg_ctx *ctx, const CountCsr &c, const rtg_config &cfg,
     bs->pc.E = cfg.tc_item_edges;
     bs->pc.R = cfg.tc_region_words;
     bs->pc.n = c.n;
-    bs->smem = (size_t)bs->W * (bs->pc.R + 1) * 4;  // region + guard word per warp
+    bs->smem = (size_t)bs->W * region_words(bs->pc.R) * 4;
     if (bs->smem + 256 > (size_t)ctx->smem_optin)
         return fail(ctx, RTG_ERR_INVALID_ARG, "schedule needs %zu B of shared memory", bs->smem);
     bs->item_cap = c.m / bs->pc.E + c.n + 1;
