@@ -18,9 +18,10 @@
 //           of the work on power-law graphs), plus a small hash table for the few elements
 //           of N+(v) below that window; out-lists with too many such elements fall back to
 //           a tile merge. It then streams the suffixes of the item's in-edges 32 at a time:
-//           whole 64-element units of each suffix with unchecked coalesced loads, then the
-//           remainders of all 32 suffixes as one flat sequence in full 32-lane windows,
-//           testing every element with one shared-memory load.
+//           whole 128-, 64- and 32-element units of each suffix with unchecked coalesced
+//           loads, then the remainders (under 32 elements) of all 32 suffixes as one flat
+//           sequence in full 32-lane windows, testing every element with one shared-memory
+//           load.
 //           Streamed elements: sum over u of d+(u)(d+(u)-1)/2, about a quarter of the
 //           push-order work on power-law graphs. The items are built once per (graph,
 //           schedule); the count (counter resets + the persistent kernel) is one CUDA graph,
@@ -197,82 +198,98 @@ __device__ __forceinline__ uint32_t bit_or_zero(uint32_t s) {
     return r;
 }
 
+// Unchecked units of one batch of 32 in-edges (lane k holds in-edge k): this lane's in-edge
+// has nu units of 32 * S elements, unit i starting at adj index base + i * 32 * S. Unit j of
+// the batch (0 <= j < U, in in-edge order) belongs to the first in-edge whose units end
+// after j: one ballot, one popcount and one shuffle per unit, no branch per in-edge. Each
+// unit is S coalesced 32-bit loads per lane; kUnitDepth units are in flight ahead of the one
+// being tested (units past the last hold idle elements).
+constexpr int kUnitDepth = 3;
+
+template <int S, class F>
+__device__ __forceinline__ uint32_t stream_units(const uint32_t *__restrict__ adjl, uint32_t nu,
+                                                 uint32_t base, int lane, uint32_t idle,
+                                                 const F &f) {
+    constexpr uint32_t kSize = 32 * S;
+    uint32_t ue = nu;  // inclusive scan: units up to and including this lane's in-edge
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t t = __shfl_up_sync(kFull, ue, o);
+        if (lane >= o) ue += t;
+    }
+    const uint32_t U = __shfl_sync(kFull, ue, 31);
+    uint32_t cnt = 0;
+    if (!U) return cnt;
+    // adj index of unit j of this lane's in-edge: ub + j * kSize (mod 2^32)
+    const uint32_t ub = base - (ue - nu) * kSize;
+    auto unit_at = [&](uint32_t j) -> const uint32_t * {
+        const int e = __popc(__ballot_sync(kFull, ue <= j));
+        return adjl + (__shfl_sync(kFull, ub, e & 31) + j * kSize);
+    };
+    uint32_t a[kUnitDepth][S];
+#pragma unroll
+    for (int d = 0; d < kUnitDepth; ++d) {
+#pragma unroll
+        for (int t = 0; t < S; ++t) a[d][t] = idle;
+        if ((uint32_t)d < U) {
+            const uint32_t *src = unit_at(d);
+#pragma unroll
+            for (int t = 0; t < S; ++t) a[d][t] = __ldg(src + 32 * t);
+        }
+    }
+    for (uint32_t j0 = 0; j0 < U; j0 += kUnitDepth) {
+#pragma unroll
+        for (int d = 0; d < kUnitDepth; ++d) {
+#pragma unroll
+            for (int t = 0; t < S; ++t) cnt += f(a[d][t]);
+            const uint32_t j = j0 + kUnitDepth + d;
+#pragma unroll
+            for (int t = 0; t < S; ++t) a[d][t] = idle;
+            if (j < U) {
+                const uint32_t *src = unit_at(j);
+#pragma unroll
+                for (int t = 0; t < S; ++t) a[d][t] = __ldg(src + 32 * t);
+            }
+        }
+    }
+    return cnt;
+}
+
 // Stream the suffix ranges of the item's in-edges [k0, k1) (edge k's range is in_rng[k]),
-// 32 in-edges at a time (lane k holds in-edge kb + k; the next batch's ranges are loaded
-// one batch ahead), and test every element with f (f(idle) must be 0). Per batch:
-//  1. units: every whole 64-element unit of every suffix, two coalesced 32-bit loads per
-//     lane and no bounds check; the warp visits only the in-edges that have units (a
-//     ballot mask), and the next unit's loads are issued before the current one is tested;
-//  2. remainders: the last (length mod 64) elements of all 32 suffixes, concatenated into
+// 32 in-edges at a time (lane k holds in-edge kb + k; `first` holds the first batch's
+// ranges, each next batch's are loaded one batch ahead), and test every element with f
+// (f(idle) must be 0). Per batch:
+//  1. units: every whole 128-element unit of every suffix (four unchecked coalesced loads
+//     per lane), then one 64-element unit where 64 or more elements are left, then one
+//     32-element unit where 32 or more are left;
+//  2. remainders: the last (length mod 32) elements of all 32 suffixes, concatenated into
 //     one sequence (in-edges with an empty remainder compacted out through `cmp`, 32
 //     entries of per-warp shared memory) and swept in 32-position windows with every lane
 //     busy: the in-edges that start inside a window are one OR-reduction of a bit per
 //     in-edge, and lane L finds its in-edge by counting the starts at or before it.
 // The per-lane count of one item fits 32 bits (at most E in-edges of at most n elements).
-constexpr uint32_t kUnit = 64;
-constexpr int kUnitDepth = 3;  // units whose loads are in flight ahead of the one tested
-constexpr int kWin = 4;        // remainder windows whose loads are in flight together
+constexpr int kWin = 4;  // remainder windows whose loads are in flight together
 
 template <class F>
 __device__ __forceinline__ uint32_t stream_item(const uint32_t *__restrict__ adj,
                                                 const uint2 *__restrict__ rng, uint32_t k0,
                                                 uint32_t k1, int lane, uint32_t idle,
-                                                uint2 *cmp, F f) {
+                                                uint2 *cmp, uint2 first, F f) {
     uint32_t cnt = 0;
     const uint32_t le = 0xFFFFFFFFu >> (31 - lane);  // lanes 0..lane
     const uint32_t lt = (1u << lane) - 1u;           // lanes below this one
     const uint32_t *adjl = adj + lane;
-    uint2 nx = (k0 + lane < k1) ? __ldg(rng + k0 + lane) : make_uint2(0u, 0u);
+    uint2 nx = first;  // ranges of the first batch, loaded by the caller
     for (uint32_t kb = k0; kb < k1; kb += 32) {
         const uint2 r = nx;
         nx = (kb + 32 + lane < k1) ? __ldg(rng + kb + 32 + lane) : make_uint2(0u, 0u);
         const uint32_t len = r.y - r.x;  // 0 past the item
-        // ---- 1. whole units
-        const uint32_t nu = len / kUnit;
-        unsigned F = __ballot_sync(kFull, nu != 0);
-        if (F) {
-            uint32_t X = 0, left = 0;
-            // next unit's first element (warp-uniform); false when the batch has none left
-            auto next_unit = [&](uint32_t &ux) -> bool {
-                if (left == 0) {
-                    if (!F) return false;
-                    const int e = __ffs(F) - 1;
-                    F &= F - 1;
-                    X = __shfl_sync(kFull, r.x, e);
-                    left = __shfl_sync(kFull, nu, e);
-                }
-                ux = X;
-                X += kUnit;
-                --left;
-                return true;
-            };
-            // kUnitDepth units in flight; a unit past the last holds idle elements
-            uint32_t a[kUnitDepth][2];
-            bool live = true;
-            auto load_unit = [&](uint32_t *u) {
-                uint32_t ux = 0;
-                if (live && next_unit(ux)) {
-                    u[0] = __ldg(adjl + ux);
-                    u[1] = __ldg(adjl + ux + 32);
-                } else {
-                    live = false;
-                    u[0] = u[1] = idle;
-                }
-            };
-#pragma unroll
-            for (int d = 0; d < kUnitDepth; ++d) load_unit(a[d]);
-            while (live) {
-#pragma unroll
-                for (int d = 0; d < kUnitDepth; ++d) {
-                    cnt += f(a[d][0]) + f(a[d][1]);
-                    load_unit(a[d]);
-                }
-            }
-#pragma unroll
-            for (int d = 0; d < kUnitDepth; ++d) cnt += f(a[d][0]) + f(a[d][1]);
-        }
+        // ---- 1. units
+        cnt += stream_units<4>(adjl, len >> 7, r.x, lane, idle, f);
+        cnt += stream_units<2>(adjl, (len >> 6) & 1u, r.x + (len & ~127u), lane, idle, f);
+        cnt += stream_units<1>(adjl, (len >> 5) & 1u, r.x + (len & ~63u), lane, idle, f);
         // ---- 2. remainders, one flat sequence
-        const uint32_t rl = len % kUnit;
+        const uint32_t rl = len & 31u;
         const unsigned Z = __ballot_sync(kFull, rl != 0);
         if (!Z) continue;
         if (rl) cmp[__popc(Z & lt)] = make_uint2(r.x + (len - rl), rl);
@@ -364,6 +381,8 @@ __global__ void __maxnreg__(48) k_tc_warp(const uint64_t *__restrict__ off, cons
         const uint64_t kin = in_off[v];
         const uint32_t k1 = min(k0 + p.E, (uint32_t)(in_off[v + 1] - kin));
         const uint32_t *Nv = adj + ov;
+        // the first batch of suffix ranges, loaded before the out-list is marked
+        const uint2 first = (k0 + lane < k1) ? __ldg(in_rng + kin + k0 + lane) : make_uint2(0u, 0u);
         const uint32_t base0 = (v + 1) & ~31u;
         // 0: bitmap only; 1: bitmap + low-part table; 2: merge
         int mode = 0;
@@ -390,12 +409,12 @@ __global__ void __maxnreg__(48) k_tc_warp(const uint64_t *__restrict__ off, cons
         const uint32_t *regp = reg - (W0 >> 5);
         const uint32_t idle = W0 + RB;
         if (mode == 0) {
-            cnt += stream_item(adj, in_rng + kin, k0, k1, lane, idle, cmp,
+            cnt += stream_item(adj, in_rng + kin, k0, k1, lane, idle, cmp, first,
                                [&](uint32_t w) -> uint32_t {
                                    return __funnelshift_r(regp[w >> 5], 0u, w) & 1u;
                                });
         } else if (mode == 1) {
-            cnt += stream_item(adj, in_rng + kin, k0, k1, lane, idle, cmp, [&](uint32_t w) -> uint32_t {
+            cnt += stream_item(adj, in_rng + kin, k0, k1, lane, idle, cmp, first, [&](uint32_t w) -> uint32_t {
                 if (w >= W0) return __funnelshift_r(regp[w >> 5], 0u, w) & 1u;
                 uint32_t sl = hash_slot(w, kLowHashLg);
                 uint32_t x = tab[sl];
