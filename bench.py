@@ -343,7 +343,7 @@ def measure_si(args, dist: Dist, ctx, cpu: bool) -> dict:
     off, el, pa, pb, exp = gen_si_workload()
     sets = ctx.sets(off, el)
     np_ = len(pa)
-    tune = sets.tune(pa, pb)  # autotuned schedule of the batched kernel (set on the context)
+    tune = None if args.no_tune else sets.tune(pa, pb)  # autotuned schedule (set on the context)
     algo = si_algo_bytes(off, pa, pb)
     for _ in range(args.warmup):
         ctx.flush_l2()
@@ -625,7 +625,9 @@ def run_gpu(args, dist: Dist) -> None:
     g.release_edges()
     info = g.info()
     m = info.m
-    tune = g.tune()  # autotuned schedule of the batched count (set on the context)
+    # autotuned schedule of the batched count (set on the context); --no-tune keeps the
+    # library default (for profiling runs: fewer launches before the timed one)
+    tune = None if args.no_tune else g.tune()
     # warm-up (also builds and captures the CUDA graph of the batched count)
     for _ in range(args.warmup):
         ctx.flush_l2()
@@ -713,7 +715,8 @@ def run_gpu(args, dist: Dist) -> None:
               "roofline": {k: r["roofline"][k] for k in ("achieved", "peak", "unit", "frac",
                                                          "traffic", "kernel", "dram_gbs",
                                                          "dram_frac") if k in r["roofline"]},
-              "gpu_launches": r["launches"], "schedule": r["schedule"]["best"]}
+              "gpu_launches": r["launches"],
+              "schedule": r["schedule"]["best"] if r["schedule"] else "library default"}
     serving = None
     if not args.tc_only and not args.no_serve and dist.rank == 0:
         r = measure_serve(args)
@@ -766,6 +769,8 @@ def main() -> None:
     ap.add_argument("--tc-only", action="store_true",
                     help="skip the batched-SI and serving summaries")
     ap.add_argument("--no-serve", action="store_true", help="skip the serving summary")
+    ap.add_argument("--no-tune", action="store_true",
+                    help="time the library's default schedules instead of autotuning first")
     args = ap.parse_args()
     if args.warmup < 3:
         ap.error("at least 3 warm-up steps")

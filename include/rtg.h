@@ -216,6 +216,12 @@ uint64_t rtg_graph_device_bytes(const rtg_graph *g);
  * does not hold is refused with RTG_ERR_FORMAT. No reference counterpart: the reference
  * rebuilds its CSR (tc/graph/graph.cpp:71-102) on every run. */
 rtg_status rtg_graph_save(rtg_ctx *ctx, const rtg_graph *g, const char *path);
+/* The checks rtg_graph_load(RTG_FMT_RTG_CSR) runs before anything reaches the device, on
+ * the host alone (no context, no GPU): RTG_OK for a file it would accept, RTG_ERR_FORMAT
+ * for a damaged or forged one (checksum, sizes, offsets, ids below n, counting-form rows
+ * ascending and above their vertex, every in-edge suffix range inside one row and holding
+ * only ranks above its head), RTG_ERR_IO when it cannot be read. */
+rtg_status rtg_graph_file_check(const char *path);
 void rtg_graph_destroy(rtg_graph *g);
 
 /* ------------------------------------------------------ triangle counting */
@@ -254,8 +260,12 @@ rtg_status rtg_tc_count_host_csr(rtg_ctx *ctx, const int32_t *offsets, const int
  * allowed. It needs no rtg_ctx.
  *
  * Input: an oriented CSR already on the current device (d_offsets: n+1 entries, d_adj: m
- * entries, rows sorted ascending, every edge stored once). Output: the exact uint64
- * triangle count written to the host word *out_total. Work is ordered on `stream`
+ * entries, rows sorted ascending, every edge stored once). The orientation must be
+ * acyclic (every edge from the lower to the higher vertex of one total order, by degree
+ * rank or by id) and hold no self loops: a cyclically oriented triangle adds nothing and a
+ * self loop adds spurious counts, and neither is detected. The library's own oriented CSR
+ * (rtg_csr_view with symmetric = 0 after rtg_csr_build) is such an input. Output: the
+ * exact uint64 triangle count written to the host word *out_total. Work is ordered on `stream`
  * (a cudaStream_t; NULL for the default stream) and the call returns when the count is
  * on the host. It uses the PLAIN kernels; their scratch lives in one fixed device array
  * inside the library (about 9 bytes per edge for RTG_NOALLOC_MAX_EDGES edges, reserved on
@@ -264,7 +274,12 @@ rtg_status rtg_tc_count_host_csr(rtg_ctx *ctx, const int32_t *offsets, const int
  *     RTG_ERR_INVALID_ARG before any GPU work, as are offsets that do not describe a CSR of
  *     m edges with ids below n;
  *   - the first call on a device looks up the array's device address (once per device, with
- *     that device current); make that first call before any stream capture;
+ *     that device current). With lazy module loading (the CUDA default) the array itself is
+ *     reserved when the library's code is first loaded on that device, which may be during
+ *     that first call: make it at start-up, before another allocator takes over the device
+ *     heap and before any stream capture;
+ *   - the looked-up address is kept for the life of the process: do not use this entry
+ *     point on a device after cudaDeviceReset (or any reset of its primary context);
  *   - every call on a device shares the one array, so calls that overlap on the GPU (other
  *     host threads, other streams) race and must be serialised by the caller.
  * Returns RTG_ERR_DEVICE on a CUDA error. It calls no cudaMalloc, cudaFree or other
@@ -297,6 +312,16 @@ void rtg_sets_destroy(rtg_sets *s);
 rtg_status rtg_si_count(rtg_ctx *ctx, const rtg_sets *s, const uint32_t *pair_a,
                         const uint32_t *pair_b, uint64_t npairs, uint32_t *out_counts,
                         uint32_t flags, rtg_timing *timing);
+/* Test hook for the bounded device waits; no counterpart in the reference (whose CUDA
+ * error path prints and exits, tc/utils/common.h:13-32). For the next batched
+ * (RTG_SI_AUTO) launch on ctx only: every shared-memory barrier wait of the staging
+ * pipeline gives up after max_polls polls instead of the default 2^22, and the first
+ * staging slot of one warp expects extra_tx_bytes (a multiple of 16) more than its copies
+ * bring. The copies all land, but that slot never completes, so its wait runs out: the
+ * warp records RTG_ERR_TIMEOUT in the status word, waits (bounded) for its other copies and
+ * returns, and the call returns RTG_ERR_TIMEOUT with the context still usable. With
+ * extra_tx_bytes = 0 only the bound changes. */
+rtg_status rtg_debug_si_wait_limit(rtg_ctx *ctx, uint32_t max_polls, uint32_t extra_tx_bytes);
 /* Dense |A| x |B| in the reference's row-major order (bs.cu:93-96,148):
  * out[(a - a_begin) * (b_end - b_begin) + (b - b_begin)]. */
 rtg_status rtg_si_count_dense(rtg_ctx *ctx, const rtg_sets *s, uint32_t a_begin,

@@ -6,14 +6,16 @@
 #
 #   REF=/path/to/RT-Graph oracle/build_ref.sh
 #
+# Without REF the checkout is looked up next to this repository (../reference).
+#
 # Reference files used (read-only): tc/graph/graph.cpp, tc/bs_tc/bs_tc.cu (its host
 # function Preprocessing; the kernels in the same file compile but never run),
 # set_intersection/data_generator/data.cpp. ThrustSortEdgesInBatch is provided on the
 # host by oracle/ref_shim.cpp. CCCL 3 no longer pulls <vector>, <algorithm> and <cassert>
 # into bs_tc.cu, so they are force-included.
 set -euo pipefail
-REF="${REF:-/root/reference}"
 HERE="$(cd "$(dirname "$0")" && pwd)"
+REF="${REF:-$HERE/../../reference}"
 OUT="$HERE/_ref"
 CUDA_HOME="${CUDA_HOME:-/usr/local/cuda}"
 if [ ! -d "$REF/tc/graph" ]; then

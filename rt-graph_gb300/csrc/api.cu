@@ -945,6 +945,13 @@ static rtg_status si_run(rtg_ctx *ctx, PairSpec &ps, const uint32_t *pair_a,
     return RTG_OK;
 }
 
+rtg_status rtg_debug_si_wait_limit(rtg_ctx *ctx, uint32_t max_polls, uint32_t extra_tx_bytes) {
+    if (!ctx || max_polls == 0 || (extra_tx_bytes & 15u)) return RTG_ERR_INVALID_ARG;
+    ctx->dbg_wait_polls = max_polls;
+    ctx->dbg_extra_tx = extra_tx_bytes;
+    return RTG_OK;
+}
+
 rtg_status rtg_si_count(rtg_ctx *ctx, const rtg_sets *s, const uint32_t *pair_a,
                         const uint32_t *pair_b, uint64_t npairs, uint32_t *out_counts,
                         uint32_t flags, rtg_timing *timing) {

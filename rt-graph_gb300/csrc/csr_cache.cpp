@@ -17,6 +17,7 @@
 // damaged or foreign file fails with RTG_ERR_FORMAT before anything reaches a kernel.
 #include <cstdio>
 #include <cstring>
+#include <string>
 #include <vector>
 
 #include "internal.h"
@@ -157,41 +158,55 @@ extern "C" rtg_status rtg_graph_save(rtg_ctx *ctx, const rtg_graph *g, const cha
 }
 
 namespace rtg {
+namespace {
 
-// Read a file written by rtg_graph_save into a new graph of ctx (no raw edges).
-rtg_status graph_load_cached(rtg_ctx *ctx, const char *path, rtg_graph **out) {
+// One CSR part of a cache file, read and checked on the host.
+struct HostCsr {
+    uint32_t n = 0, max_deg = 0, has_src = 0;
+    uint64_t m = 0, work = 0;
+    std::vector<uint64_t> off, in_off;
+    std::vector<uint32_t> adj, src;
+    std::vector<uint2> rng;
+};
+
+struct CacheFile {
+    uint32_t parts = 0;
+    uint64_t m_input = 0;
+    int32_t orient = -1;
+    HostCsr ori, cnt, sym;
+};
+
+// Read and check a file written by rtg_graph_save, on the host only (no device, no
+// context). RTG_ERR_IO when it cannot be opened, RTG_ERR_FORMAT with the reason in `why`
+// when it is not a valid cache file.
+rtg_status read_cache_file(const char *path, CacheFile &cf, std::string &why) {
     FILE *f = std::fopen(path, "rb");
-    if (!f) return fail(ctx, RTG_ERR_IO, "cannot open %s", path);
+    if (!f) {
+        why = "cannot open file";
+        return RTG_ERR_IO;
+    }
     std::fseek(f, 0, SEEK_END);
     const long long size = std::ftell(f);
     std::fseek(f, 0, SEEK_SET);
     char magic[8] = {};
     if (size < 8 + 8 || std::fread(magic, 1, 8, f) != 8 || std::memcmp(magic, kMagic, 8)) {
         std::fclose(f);
-        return fail(ctx, RTG_ERR_FORMAT, "%s is not a CSR cache file", path);
+        why = "not a CSR cache file";
+        return RTG_ERR_FORMAT;
     }
     Reader r{f, 1469598103934665603ull, (uint64_t)size - 8 - 8};  // checksum excluded
-    uint32_t version = 0, parts = 0, zero = 0;
-    uint64_t m_input = 0;
-    int32_t orient = -1;
+    uint32_t version = 0, zero = 0;
     r.val(version);
-    r.val(parts);
-    r.val(m_input);
-    r.val(orient);
+    r.val(cf.parts);
+    r.val(cf.m_input);
+    r.val(cf.orient);
     r.val(zero);
-    auto bad = [&](const char *why) {
+    auto bad = [&](const char *w) {
         std::fclose(f);
-        return fail(ctx, RTG_ERR_FORMAT, "%s: %s", path, why);
+        why = w;
+        return RTG_ERR_FORMAT;
     };
-    if (!r.ok || version != kVersion || !parts || (parts & ~7u)) return bad("bad header");
-    // every array is read and checked on the host before any device allocation
-    struct HostCsr {
-        uint32_t n = 0, max_deg = 0, has_src = 0;
-        uint64_t m = 0, work = 0;
-        std::vector<uint64_t> off, in_off;
-        std::vector<uint32_t> adj, src;
-        std::vector<uint2> rng;
-    } ho, hc, hs;
+    if (!r.ok || version != kVersion || !cf.parts || (cf.parts & ~7u)) return bad("bad header");
     auto read_csr = [&](HostCsr &c, bool with_src, bool with_work) -> bool {
         if (!r.val(c.n) || !r.val(c.max_deg) || !r.val(c.m)) return false;
         if (with_work && !r.val(c.work)) return false;
@@ -209,8 +224,9 @@ rtg_status graph_load_cached(rtg_ctx *ctx, const char *path, rtg_graph **out) {
         return valid_offsets(c.off, c.n, c.m) && valid_ids(c.adj, c.m, c.n) &&
                (!c.has_src || valid_ids(c.src, c.m, c.n));
     };
-    if ((parts & kPartOri) && !read_csr(ho, true, true)) return bad("oriented CSR");
-    if (parts & kPartCnt) {
+    if ((cf.parts & kPartOri) && !read_csr(cf.ori, true, true)) return bad("oriented CSR");
+    if (cf.parts & kPartCnt) {
+        HostCsr &hc = cf.cnt;
         if (!read_csr(hc, false, false)) return bad("counting CSR");
         const uint64_t need = (hc.n + 1ull) * 8 + hc.m * 8;
         if (need > r.left) return bad("counting CSR");
@@ -219,9 +235,10 @@ rtg_status graph_load_cached(rtg_ctx *ctx, const char *path, rtg_graph **out) {
         if (!r.get(hc.in_off.data(), (hc.n + 1ull) * 8) || !r.get(hc.rng.data(), hc.m * 8))
             return bad("counting CSR");
         if (!valid_offsets(hc.in_off, hc.n, hc.m)) return bad("counting CSR in-edges");
-        // the batched kernel indexes its per-warp bitmap by (element - v - 1): every row of
-        // v must hold ascending ranks above v, and every suffix range of an in-edge of v
-        // must lie inside one row and hold only ranks above v
+        // the batched kernel indexes its per-warp bitmap by (element - window origin) and
+        // takes every element of a suffix of an in-edge of v to be a rank above v: every
+        // row of v must hold ascending ranks above v, and every suffix range of an in-edge
+        // of v must lie inside one row and hold only ranks above v
         for (uint64_t v = 0; v < hc.n; ++v)
             for (uint64_t q = hc.off[v]; q < hc.off[v + 1]; ++q)
                 if (hc.adj[q] <= v || (q > hc.off[v] && hc.adj[q] <= hc.adj[q - 1]))
@@ -242,12 +259,26 @@ rtg_status graph_load_cached(rtg_ctx *ctx, const char *path, rtg_graph **out) {
                     return bad("suffix range");
             }
     }
-    if ((parts & kPartSym) && !read_csr(hs, false, true)) return bad("symmetric CSR");
+    if ((cf.parts & kPartSym) && !read_csr(cf.sym, false, true)) return bad("symmetric CSR");
     uint64_t want = 0, h = r.h;
     if (!r.ok || r.left != 0 || std::fread(&want, 1, 8, f) != 8 || want != h)
         return bad("checksum mismatch or trailing bytes");
     std::fclose(f);
+    return RTG_OK;
+}
 
+}  // namespace
+
+// Read a file written by rtg_graph_save into a new graph of ctx (no raw edges).
+rtg_status graph_load_cached(rtg_ctx *ctx, const char *path, rtg_graph **out) {
+    CacheFile cf;
+    std::string why;
+    const rtg_status rs = read_cache_file(path, cf, why);
+    if (rs != RTG_OK) return fail(ctx, rs, "%s: %s", path, why.c_str());
+    const uint32_t parts = cf.parts;
+    const uint64_t m_input = cf.m_input;
+    const int32_t orient = cf.orient;
+    HostCsr &ho = cf.ori, &hc = cf.cnt, &hs = cf.sym;
     rtg_graph *g = nullptr;
     // an empty edge list gives a graph with no raw edges to which the CSRs are attached
     RTG_TRY(rtg_graph_from_host_edges(ctx, nullptr, nullptr, 0, &g));
@@ -287,3 +318,10 @@ rtg_status graph_load_cached(rtg_ctx *ctx, const char *path, rtg_graph **out) {
 }
 
 }  // namespace rtg
+
+extern "C" rtg_status rtg_graph_file_check(const char *path) {
+    if (!path) return RTG_ERR_INVALID_ARG;
+    rtg::CacheFile cf;
+    std::string why;
+    return rtg::read_cache_file(path, cf, why);
+}

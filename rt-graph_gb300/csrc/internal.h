@@ -68,6 +68,8 @@ struct rtg_ctx {
     std::string last_error;
     rtg_config cfg{};
     uint64_t launches = 0;
+    // test hook (rtg_debug_si_wait_limit): applied to the next batched SI launch, then reset
+    uint32_t dbg_wait_polls = 0, dbg_extra_tx = 0;
     int sm_count = 0;
     int smem_optin = 0;
     int cc_major = 0, cc_minor = 0;

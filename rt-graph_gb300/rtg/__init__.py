@@ -133,6 +133,7 @@ _SIGS = {
     "rtg_csr_to_host": (C.c_int, [P, P, C.c_int, P, P]),
     "rtg_graph_release_edges": (C.c_int, [P]),
     "rtg_graph_device_bytes": (C.c_uint64, [P]),
+    "rtg_graph_file_check": (C.c_int, [C.c_char_p]),
     "rtg_graph_save": (C.c_int, [P, P, C.c_char_p]),
     "rtg_graph_destroy": (None, [P]),
     "rtg_tc_count": (C.c_int, [P, P, C.c_int, u64p, C.POINTER(Timing)]),
@@ -142,6 +143,7 @@ _SIGS = {
                                         C.POINTER(Timing)]),
     "rtg_graph_pair_count": (C.c_int, [P, P, P, P, C.c_uint64, P, C.c_uint32,
                                        C.POINTER(Timing)]),
+    "rtg_debug_si_wait_limit": (C.c_int, [P, C.c_uint32, C.c_uint32]),
     "rtg_tc_count_device_csr_noalloc": (C.c_int, [P, P, C.c_uint32, C.c_uint64, u64p, P]),
     "rtg_sets_from_host": (C.c_int, [P, P, C.c_uint64, P, C.POINTER(P)]),
     "rtg_sets_from_host_u32": (C.c_int, [P, P, C.c_uint32, P, C.POINTER(P)]),

@@ -205,3 +205,23 @@ def test_vertex_pair_queries_on_graph(ctx):
     v = rng.integers(0, n, 30000).astype(np.uint32)
     got, _ = g.pair_count(u, v)
     assert np.array_equal(got, oracle.si_pairs(off, adj, u, v))
+
+
+def test_bounded_wait_runs_out_cleanly(ctx):
+    """A staging-slot wait that cannot complete (the test hook makes one slot expect 16
+    bytes more than its copies bring; every copy still lands, nothing stays in flight)
+    gives up after a short bound: the call returns RTG_ERR_TIMEOUT, nothing faults or
+    hangs, and the next call on the same context is exact."""
+    off, el, pa, pb, exp = rtg.gen_si_pairs(20_000, seed=9)
+    sets = ctx.sets(off, el)
+    out = np.empty(len(pa), np.uint32)
+    assert rtg.lib.rtg_debug_si_wait_limit(ctx.h, 256, 15) == rtg.ERR_INVALID_ARG
+    assert rtg.lib.rtg_debug_si_wait_limit(ctx.h, 256, 16) == rtg.OK
+    st = rtg.lib.rtg_si_count(ctx.h, sets.h, rtg._ptr(pa), rtg._ptr(pb), len(pa),
+                              rtg._ptr(out), rtg.SI_AUTO, None)
+    assert st == rtg.ERR_TIMEOUT
+    assert b"bounded device wait" in rtg.lib.rtg_last_error(ctx.h)
+    for _ in range(2):  # the hook applied to one launch only; the context stays usable
+        got, _ = sets.count(pa, pb, rtg.SI_AUTO)
+        assert np.array_equal(got, exp)
+    sets.close()

@@ -62,9 +62,34 @@ def test_noalloc_alternating_graphs_reuse_the_array(ctx):
             assert g.tc(rtg.TC_PLAIN)[0] == want
 
 
-def test_noalloc_rejects_graphs_beyond_its_limit():
+def test_noalloc_rejects_graphs_beyond_its_limit(ctx):
+    """Real device arrays with an edge count one past the limit: refused before any GPU
+    work; the same arrays with their true sizes then count correctly."""
+    rec = tc_golden()["rmat_s12_ef16_s1"]
+    s, d = golden_edges(rec)
+    g = ctx.graph_from_edges(s, d).build(rtg.ORIENT_DEGREE)
+    off, adj, n, m = _device_csr(g)
     out = C.c_uint64(7)
-    st = rtg.lib.rtg_tc_count_device_csr_noalloc(None, None, 10, (1 << 19) + 1, C.byref(out), None)
+    st = rtg.lib.rtg_tc_count_device_csr_noalloc(off, adj, n, (1 << 19) + 1, C.byref(out), None)
     assert st == rtg.ERR_INVALID_ARG
+    assert _noalloc_count(off, adj, n, m) == rec["triangles"]
     st = rtg.lib.rtg_tc_count_device_csr_noalloc(None, None, 0, 0, C.byref(out), None)
     assert st == rtg.OK and out.value == 0
+
+
+def test_noalloc_rejects_sizes_that_do_not_describe_the_csr(ctx):
+    """The device-side check of the offsets and ids: an edge count below the CSR's (the
+    offsets end past m) and a vertex count at or below the largest stored id are refused with
+    RTG_ERR_INVALID_ARG (every read stays inside the real arrays, which are larger); the
+    shared scratch array then still gives the right count."""
+    rec = tc_golden()["rmat_s12_ef16_s1"]
+    s, d = golden_edges(rec)
+    g = ctx.graph_from_edges(s, d).build(rtg.ORIENT_DEGREE)
+    off, adj, n, m = _device_csr(g)
+    top = int(g.csr()[1].max())  # the largest id stored: a vertex count of `top` excludes it
+    out = C.c_uint64(7)
+    for bad_n, bad_m in ((n, m - 1), (top, m), (top, m - 1)):
+        st = rtg.lib.rtg_tc_count_device_csr_noalloc(off, adj, bad_n, bad_m, C.byref(out), None)
+        assert st == rtg.ERR_INVALID_ARG, (bad_n, bad_m)
+    for _ in range(2):
+        assert _noalloc_count(off, adj, n, m) == rec["triangles"]
