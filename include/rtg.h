@@ -314,13 +314,12 @@ rtg_status rtg_si_count(rtg_ctx *ctx, const rtg_sets *s, const uint32_t *pair_a,
                         uint32_t flags, rtg_timing *timing);
 /* Test hook for the bounded device waits; no counterpart in the reference (whose CUDA
  * error path prints and exits, tc/utils/common.h:13-32). For the next batched
- * (RTG_SI_AUTO) launch on ctx only: every shared-memory barrier wait of the staging
- * pipeline gives up after max_polls polls instead of the default 2^22, and the first
- * staging slot of one warp expects extra_tx_bytes (a multiple of 16) more than its copies
- * bring. The copies all land, but that slot never completes, so its wait runs out: the
- * warp records RTG_ERR_TIMEOUT in the status word, waits (bounded) for its other copies and
- * returns, and the call returns RTG_ERR_TIMEOUT with the context still usable. With
- * extra_tx_bytes = 0 only the bound changes. */
+ * (RTG_SI_AUTO) launch on ctx only: one warp of the staging kernel arms its shared-memory
+ * barrier for extra_tx_bytes (a multiple of 16, not 0) that no copy brings, so that phase
+ * never completes and its wait, bounded at max_polls polls (the kernel's waits default to
+ * 2^22), runs out. The warp records RTG_ERR_TIMEOUT in the status word and leaves before
+ * taking any pairs (the other warps count them all, with nothing in flight), and the call
+ * returns RTG_ERR_TIMEOUT with the context still usable. */
 rtg_status rtg_debug_si_wait_limit(rtg_ctx *ctx, uint32_t max_polls, uint32_t extra_tx_bytes);
 /* Dense |A| x |B| in the reference's row-major order (bs.cu:93-96,148):
  * out[(a - a_begin) * (b_end - b_begin) + (b - b_begin)]. */

@@ -946,7 +946,8 @@ static rtg_status si_run(rtg_ctx *ctx, PairSpec &ps, const uint32_t *pair_a,
 }
 
 rtg_status rtg_debug_si_wait_limit(rtg_ctx *ctx, uint32_t max_polls, uint32_t extra_tx_bytes) {
-    if (!ctx || max_polls == 0 || (extra_tx_bytes & 15u)) return RTG_ERR_INVALID_ARG;
+    if (!ctx || max_polls == 0 || extra_tx_bytes == 0 || (extra_tx_bytes & 15u))
+        return RTG_ERR_INVALID_ARG;
     ctx->dbg_wait_polls = max_polls;
     ctx->dbg_extra_tx = extra_tx_bytes;
     return RTG_OK;

@@ -175,9 +175,8 @@ struct StreamCfg {
     uint32_t cnt_off;
     uint32_t ring_off;
     uint32_t ratio;       // a pair longer than a slot is searched when |B| > ratio * |A|
-    uint32_t wait_polls;  // bound of every mbarrier wait (polls)
-    uint32_t extra_tx;    // test hook: bytes the first slot of warp 0 in block 0 expects on
-                          // top of its copies (0 in normal use)
+    uint32_t probe_polls;  // test hook (0 in normal use): see the start of k_si_stream
+    uint32_t probe_tx;
 };
 
 // Per-slot job description in shared memory (32-bit words):
@@ -295,9 +294,16 @@ __global__ void k_si_stream(SiArgs s, uint32_t *out, unsigned long long *head, S
     fence_mbar_init();
     __syncwarp();
     const uint32_t CAPE = p.slot_words - 16;  // list elements per chunk job (room for alignment)
-    // test hook: the first slot this warp arms expects extra bytes that no copy brings, so
-    // its wait runs out (bounded) while every copy still lands
-    uint32_t inj = (blockIdx.x == 0 && warp == 0) ? p.extra_tx : 0u;
+    if (p.probe_tx && blockIdx.x == 0 && warp == 0) {
+        // test hook: this warp arms its first slot for probe_tx bytes that no copy brings,
+        // so the phase never completes and the wait (bounded at probe_polls) runs out; the
+        // warp records the timeout and leaves before taking any pairs (the other warps count
+        // them all), with nothing in flight
+        if (lane == 0) mbar_arrive_expect_tx(bars, p.probe_tx);
+        __syncwarp();
+        if (!mbar_wait(bars, 0u, p.probe_polls) && lane == 0) atomicExch(status, kStatusTimeout);
+        return;
+    }
 
     // One batch of 32 pairs, lane e holding pair base + e: its lists, its kind, the words
     // its widened lists take in a slot and inclusive warp scans of those words, of the
@@ -424,9 +430,8 @@ __global__ void k_si_stream(SiArgs s, uint32_t *out, unsigned long long *head, S
                     mt[5] = LS;
                     mt[kP + nseg] = L;
                     mt[kS + nseg] = LS;
-                    mbar_arrive_expect_tx(bar, tx + inj);
+                    mbar_arrive_expect_tx(bar, tx);
                 }
-                inj = 0;
                 __syncwarp();
                 if (copies) {
                     const uintptr_t gaa = reinterpret_cast<uintptr_t>(cur.r.A) & ~(uintptr_t)15;
@@ -502,11 +507,10 @@ __global__ void k_si_stream(SiArgs s, uint32_t *out, unsigned long long *head, S
             mt[kOffB] = resA / 4 + hB;
             mt[kLenB] = nbb;
             mt[kOut] = 0;
-            mbar_arrive_expect_tx(bar, bytesA + bytesB + inj);
+            mbar_arrive_expect_tx(bar, bytesA + bytesB);
             bulk_copy_g2s(slot, reinterpret_cast<const void *>(gaa), bytesA, bar);
             bulk_copy_g2s(slot + resA / 4, reinterpret_cast<const void *>(gbb), bytesB, bar);
         }
-        inj = 0;
         return true;
     };
 
@@ -523,11 +527,11 @@ __global__ void k_si_stream(SiArgs s, uint32_t *out, unsigned long long *head, S
         }
         if (inflight == 0) break;
         __syncwarp();
-        if (!mbar_wait(bars + sr, (phase >> sr) & 1u, p.wait_polls)) {
+        if (!mbar_wait(bars + sr, (phase >> sr) & 1u)) {
             if (lane == 0) atomicExch(status, kStatusTimeout);
             for (uint32_t q = 1; q < inflight; ++q) {  // bounded drain of the others
                 const uint32_t s2 = (sr + q) % p.S;
-                mbar_wait(bars + s2, (phase >> s2) & 1u, p.wait_polls);
+                mbar_wait(bars + s2, (phase >> s2) & 1u);
             }
             break;
         }
@@ -649,8 +653,8 @@ rtg_status si_count_device(rtg_ctx *ctx, const PairSpec &ps, uint32_t *d_out, ui
         sc.slot_words = slot_bytes / 4;
         sc.ratio = cf.si_search_ratio ? cf.si_search_ratio : kDefaultStreamRatio;
         // the test hook of rtg_debug_si_wait_limit applies to one launch
-        sc.wait_polls = ctx->dbg_wait_polls ? ctx->dbg_wait_polls : kMaxWaitIters;
-        sc.extra_tx = ctx->dbg_extra_tx;
+        sc.probe_polls = ctx->dbg_wait_polls ? ctx->dbg_wait_polls : kMaxWaitIters;
+        sc.probe_tx = ctx->dbg_extra_tx;
         ctx->dbg_wait_polls = ctx->dbg_extra_tx = 0;
         sc.meta_off = ((W * sc.S * 8) + 127u) & ~127u;
         sc.cnt_off = (sc.meta_off + W * sc.S * kMetaWords * 4 + 127u) & ~127u;
