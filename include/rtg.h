@@ -36,7 +36,7 @@
 extern "C" {
 #endif
 
-#define RTG_ABI_VERSION 1
+#define RTG_ABI_VERSION 2
 
 /* Status codes. The reference prints and calls exit(2) on any CUDA error
  * (tc/utils/common.h:13-32); librtg returns one of these instead. */
@@ -158,6 +158,11 @@ typedef struct rtg_config {
     uint32_t si_stage_slots;    /* bulk-copy staging slots per warp (2..16)           */
     uint32_t si_stage_bytes;    /* bytes per staging slot (multiple of 128, 512..32768) */
     uint32_t si_blocks_per_sm;  /* resident blocks per SM of the batched SI kernel    */
+    uint32_t si_skew_stream;    /* 1: a skewed pair longer than a staging slot whose short
+                                   list fits a slot's table is counted by staging the short
+                                   list in shared memory (bulk copy) and streaming the long
+                                   list from HBM in 16-byte loads, when that reads fewer
+                                   sectors than searching it; 0 (default): always searched */
 } rtg_config;
 
 /* ---------------------------------------------------------------- context */

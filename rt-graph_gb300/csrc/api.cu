@@ -167,6 +167,8 @@ void rtg_destroy(rtg_ctx *ctx) {
     for (auto &b : ctx->scratch) dev_free(b.ptr);
     for (auto &b : ctx->work) dev_free(b.ptr);
     dev_free(ctx->flush_buf);
+    if (ctx->si_exec) cudaGraphExecDestroy(ctx->si_exec);
+    if (ctx->si_graph) cudaGraphDestroy(ctx->si_graph);
     dev_free(ctx->d_status);
     dev_free(ctx->d_scalars);
     for (auto &ev : ctx->ev)
@@ -189,6 +191,8 @@ rtg_status rtg_set_config(rtg_ctx *ctx, const rtg_config *cfg) {
                                 cfg->si_stage_bytes > 32768))
         return fail(ctx, RTG_ERR_INVALID_ARG,
                     "si_stage_bytes must be a multiple of 128 in [512, 32768]");
+    if (cfg->si_skew_stream > 1)
+        return fail(ctx, RTG_ERR_INVALID_ARG, "si_skew_stream must be 0 or 1");
     ctx->cfg = *cfg;
     return RTG_OK;
 }

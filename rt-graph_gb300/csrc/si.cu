@@ -175,6 +175,8 @@ struct StreamCfg {
     uint32_t cnt_off;
     uint32_t ring_off;
     uint32_t ratio;       // a pair longer than a slot is searched when |B| > ratio * |A|
+    uint32_t skew_pa;     // skewed pairs whose short list has at most this many elements
+                          // are staged and streamed (skew jobs); longer ones are searched
     uint32_t probe_polls;  // test hook (0 in normal use): see the start of k_si_stream
     uint32_t probe_tx;
 };
@@ -203,7 +205,60 @@ __device__ __forceinline__ uint32_t smem_lower_bound(const uint32_t *B, uint32_t
     }
     return (uint32_t)(first - B) + ((*first < x) ? 1u : 0u);
 }
-enum : uint32_t { kJobPacked = 0, kJobChunk = 1, kJobChunkLast = 2 };
+enum : uint32_t { kJobPacked = 0, kJobChunk = 1, kJobChunkLast = 2, kJobSkew = 3 };
+// Meta words of a skew job (its other fields stay 0): short list length and word offset in
+// the slot, long list address (two words) and length, hash table word offset and log2 size.
+constexpr uint32_t kSkA = 6, kSkOffA = 7, kSkB = 42, kSkLenB = 44, kSkTab = 45, kSkLg = 46;
+
+// |A ∩ B| for the short list A staged in a slot and the long list B read from global
+// memory: A goes into an open-addressing table in the same slot (2^lg words, kEmpty marks
+// an empty slot, load at most 1/4), then B streams from HBM in coalesced 16-byte loads (its
+// first and last few elements off the 16-byte grid as single words), every element probed
+// in the table. Lane-local partial count.
+__device__ __forceinline__ uint32_t skew_probe(const uint32_t *tab, uint32_t lg, uint32_t w) {
+    const uint32_t mask = (1u << lg) - 1;
+    uint32_t sl = hash_slot(w, lg);
+    uint32_t x = tab[sl];
+    while (x != w && x != kEmpty) {
+        sl = (sl + 1) & mask;
+        x = tab[sl];
+    }
+    return x == w ? 1u : 0u;
+}
+
+__device__ __forceinline__ uint32_t skew_stream_count(const uint32_t *As, uint32_t na,
+                                                      uint32_t *tab, uint32_t lg,
+                                                      const uint32_t *__restrict__ B, uint32_t nb,
+                                                      int lane) {
+    const uint32_t cap = 1u << lg;
+    for (uint32_t q = lane; q < cap; q += 32) tab[q] = kEmpty;
+    __syncwarp();
+    for (uint32_t q = lane; q < na; q += 32) {
+        const uint32_t w = As[q];
+        uint32_t sl = hash_slot(w, lg);
+        while (atomicCAS(&tab[sl], kEmpty, w) != kEmpty) sl = (sl + 1) & (cap - 1);
+    }
+    __syncwarp();
+    uint32_t c = 0;
+    const uint32_t head = min(nb, (uint32_t)((16u - (reinterpret_cast<uintptr_t>(B) & 15u)) & 15u) >> 2);
+    if ((uint32_t)lane < head) c += skew_probe(tab, lg, __ldg(B + lane));
+    const uint4 *B4 = reinterpret_cast<const uint4 *>(B + head);
+    const uint32_t n4 = (nb - head) >> 2;
+    for (uint32_t i = lane; i < n4; i += 64) {
+        const uint4 v = __ldg(B4 + i);
+        const bool two = i + 32 < n4;
+        uint4 u = make_uint4(0u, 0u, 0u, 0u);
+        if (two) u = __ldg(B4 + i + 32);
+        c += skew_probe(tab, lg, v.x) + skew_probe(tab, lg, v.y) + skew_probe(tab, lg, v.z) +
+             skew_probe(tab, lg, v.w);
+        if (two)
+            c += skew_probe(tab, lg, u.x) + skew_probe(tab, lg, u.y) +
+                 skew_probe(tab, lg, u.z) + skew_probe(tab, lg, u.w);
+    }
+    const uint32_t t0 = head + 4 * n4;
+    if (t0 + lane < nb) c += skew_probe(tab, lg, __ldg(B + t0 + lane));
+    return c;
+}
 enum : uint32_t { kPairZero = 0, kPairPacked = 1, kPairChunked = 2, kPairSkewed = 3 };
 
 // Count the common elements met on diagonals [x0, x1) of the merge of two sorted unique
@@ -279,7 +334,7 @@ __device__ __forceinline__ uint32_t skew_search_count(const uint32_t *__restrict
     return c;
 }
 
-__global__ void k_si_stream(SiArgs s, uint32_t *out, unsigned long long *head, StreamCfg p,
+__global__ void __maxnreg__(80) k_si_stream(SiArgs s, uint32_t *out, unsigned long long *head, StreamCfg p,
                             uint32_t *status) {
     extern __shared__ __align__(128) unsigned char stage_smem[];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -449,6 +504,37 @@ __global__ void k_si_stream(SiArgs s, uint32_t *out, unsigned long long *head, S
             b = __shfl_sync(kFull, cur.r.b, e);
             pk = cur.base + e;
             ++e;
+            // skewed: stream the long list when that reads fewer sectors than searching it
+            // (about b / 8 sectors against about one sector per search step, a x (log2 b - 4)
+            // of them after the bucket maxima), else search it from global memory
+            if (kind == kPairSkewed && a <= p.skew_pa && b < 8u * a * (27u - __clz(b))) {
+                // short list staged in the slot by a bulk copy; the long list is streamed
+                // by the consumer (skew_stream_count)
+                if (lane == 0) {
+                    const uintptr_t ga = reinterpret_cast<uintptr_t>(LA);
+                    const uintptr_t gaa = ga & ~(uintptr_t)15;
+                    const uint32_t hA = (uint32_t)(ga - gaa) >> 2;
+                    const uint32_t bytesA = ((hA + a) * 4u + 15u) & ~15u;
+                    uint32_t lg = 5;
+                    while ((1u << lg) < 4 * a) ++lg;
+                    mt[0] = 0;
+                    mt[1] = kJobSkew;
+                    mt[2] = (uint32_t)pk;
+                    mt[3] = (uint32_t)(pk >> 32);
+                    mt[4] = 0;
+                    mt[5] = 0;
+                    mt[kSkA] = a;
+                    mt[kSkOffA] = hA;
+                    mt[kSkB] = (uint32_t)reinterpret_cast<uintptr_t>(LB);
+                    mt[kSkB + 1] = (uint32_t)(reinterpret_cast<uintptr_t>(LB) >> 32);
+                    mt[kSkLenB] = b;
+                    mt[kSkTab] = p.skew_pa + 4;
+                    mt[kSkLg] = lg;
+                    mbar_arrive_expect_tx(bar, bytesA);
+                    bulk_copy_g2s(slot, reinterpret_cast<const void *>(gaa), bytesA, bar);
+                }
+                return true;
+            }
             if (kind == kPairSkewed) {
                 uint32_t c = skew_search_count(LA, a, LB, b, lane);
                 c = __reduce_add_sync(kFull, c);
@@ -579,7 +665,14 @@ __global__ void k_si_stream(SiArgs s, uint32_t *out, unsigned long long *head, S
         }
         __syncwarp();
         const uint64_t obase = (uint64_t)mt[2] | ((uint64_t)mt[3] << 32);
-        if (kind == kJobPacked) {
+        if (kind == kJobSkew) {
+            const uint32_t *LBp = reinterpret_cast<const uint32_t *>(
+                (uint64_t)mt[kSkB] | ((uint64_t)mt[kSkB + 1] << 32));
+            uint32_t c = skew_stream_count(slot + mt[kSkOffA], mt[kSkA], slot + mt[kSkTab],
+                                           mt[kSkLg], LBp, mt[kSkLenB], lane);
+            c = __reduce_add_sync(kFull, c);
+            if (lane == 0) out[obase] = c;
+        } else if (kind == kJobPacked) {
             if ((uint32_t)lane < nseg) {
                 out[obase + mt[kOut + lane]] = cnt[lane];
                 cnt[lane] = 0;
@@ -652,6 +745,13 @@ rtg_status si_count_device(rtg_ctx *ctx, const PairSpec &ps, uint32_t *d_out, ui
         const uint32_t slot_bytes = cf.si_stage_bytes ? cf.si_stage_bytes : kDefaultStageBytes;
         sc.slot_words = slot_bytes / 4;
         sc.ratio = cf.si_search_ratio ? cf.si_search_ratio : kDefaultStreamRatio;
+        // a skew job holds the short list (at most skew_pa elements, widened) and a table
+        // of 4 x skew_pa words after it: the largest power of two with 5 x + 20 <= slot words
+        sc.skew_pa = 0;
+        if (cf.si_skew_stream) {
+            sc.skew_pa = 16;
+            while (5 * (2 * sc.skew_pa) + 20 <= sc.slot_words) sc.skew_pa *= 2;
+        }
         // the test hook of rtg_debug_si_wait_limit applies to one launch
         sc.probe_polls = ctx->dbg_wait_polls ? ctx->dbg_wait_polls : kMaxWaitIters;
         sc.probe_tx = ctx->dbg_extra_tx;
@@ -671,11 +771,48 @@ rtg_status si_count_device(rtg_ctx *ctx, const PairSpec &ps, uint32_t *d_out, ui
         const uint64_t need = (ps.npairs + 32ull * W - 1) / (32ull * W);
         const int grid = (int)std::max<uint64_t>(1, std::min<uint64_t>(need, (uint64_t)ctx->sm_count * per_sm));
         unsigned long long *head = ctx->d_scalars + 8;
-        RTG_CUDA(ctx, cudaMemsetAsync(head, 0, 8, ctx->stream));
+        // one CUDA graph per context: the queue-head reset and the persistent kernel, captured
+        // on the first launch; later launches set the kernel node's grid, shared memory and
+        // arguments (pairs, outputs, schedule) and replay it
+        SiArgs args = make_args(ps);
+        uint32_t *status = ctx->d_status;
+        if (!ctx->si_exec) {
+            cudaGraph_t gr = nullptr;
+            RTG_CUDA(ctx, cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
+            cudaMemsetAsync(head, 0, 8, ctx->stream);
+            k_si_stream<<<grid, W * 32, smem, ctx->stream>>>(args, d_out, head, sc, status);
+            const cudaError_t ce = cudaStreamEndCapture(ctx->stream, &gr);
+            if (ce != cudaSuccess) return cuda_fail(ctx, ce, "SI graph capture", __FILE__, __LINE__);
+            cudaGraphExec_t ex = nullptr;
+            const cudaError_t ie = cudaGraphInstantiate(&ex, gr, 0);
+            if (ie != cudaSuccess) {
+                cudaGraphDestroy(gr);
+                return cuda_fail(ctx, ie, "SI graph instantiate", __FILE__, __LINE__);
+            }
+            size_t nn = 0;
+            cudaGraphGetNodes(gr, nullptr, &nn);
+            std::vector<cudaGraphNode_t> nodes(nn);
+            cudaGraphGetNodes(gr, nodes.data(), &nn);
+            for (auto nd : nodes) {
+                cudaGraphNodeType t;
+                if (cudaGraphNodeGetType(nd, &t) == cudaSuccess && t == cudaGraphNodeTypeKernel)
+                    ctx->si_knode = nd;
+            }
+            ctx->si_graph = gr;
+            ctx->si_exec = ex;
+            if (!ctx->si_knode) return fail(ctx, RTG_ERR_DEVICE, "SI graph has no kernel node");
+        } else {
+            void *kargs[] = {&args, &d_out, &head, &sc, &status};
+            cudaKernelNodeParams kp{};
+            kp.func = reinterpret_cast<void *>(k_si_stream);
+            kp.gridDim = dim3((unsigned)grid);
+            kp.blockDim = dim3(W * 32);
+            kp.sharedMemBytes = (unsigned)smem;
+            kp.kernelParams = kargs;
+            RTG_CUDA(ctx, cudaGraphExecKernelNodeSetParams(ctx->si_exec, ctx->si_knode, &kp));
+        }
         RTG_CUDA(ctx, cudaEventRecord(ctx->ev[6], ctx->stream));
-        k_si_stream<<<grid, W * 32, smem, ctx->stream>>>(make_args(ps), d_out, head, sc,
-                                                         ctx->d_status);
-        RTG_CUDA(ctx, cudaGetLastError());
+        RTG_CUDA(ctx, cudaGraphLaunch(ctx->si_exec, ctx->stream));
         RTG_CUDA(ctx, cudaEventRecord(ctx->ev[7], ctx->stream));
         (*launches)++;
         if (kernel_ms) {

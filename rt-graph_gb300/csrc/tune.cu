@@ -232,7 +232,7 @@ extern "C" rtg_status rtg_tune_si(rtg_ctx *ctx, const rtg_sets *s, const uint32_
     // the TC fields of the context's schedule are kept as they are
     rtg_config def = saved;
     def.si_block_warps = def.si_search_ratio = def.si_stage_slots = def.si_stage_bytes = 0;
-    def.si_blocks_per_sm = 0;
+    def.si_blocks_per_sm = def.si_skew_stream = 0;
     double def_ms = 0;
     rtg_status st = run(def, dwant, &def_ms);
     if (st != RTG_OK) {
@@ -269,6 +269,21 @@ extern "C" rtg_status rtg_tune_si(rtg_ctx *ctx, const rtg_sets *s, const uint32_
                         best = c;
                     }
                 }
+    {
+        // the best schedule with skewed pairs staged and streamed instead of searched
+        rtg_config c = best;
+        c.si_skew_stream = 1;
+        double ms = 0;
+        res->candidates++;
+        if (run(c, dgot, &ms) != RTG_OK ||
+            cudaMemcpy(hg.data(), dgot, npairs * 4, cudaMemcpyDeviceToHost) != cudaSuccess ||
+            hg != hw) {
+            res->rejected++;
+        } else if (ms < best_ms) {
+            best_ms = ms;
+            best = c;
+        }
+    }
     ctx->last_error.clear();
     rtg_set_config(ctx, &best);
     res->best = best;

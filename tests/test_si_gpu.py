@@ -103,6 +103,9 @@ def test_generated_workload_known_answers(ctx, family):
     # 1000: nearly every pair merged or chunked
     dict(si_search_ratio=1), dict(si_search_ratio=1000),
     dict(si_search_ratio=2, si_stage_bytes=1024, si_stage_slots=3),
+    # skewed pairs staged and streamed (short list in the slot, long list in 16-byte loads)
+    dict(si_skew_stream=1), dict(si_skew_stream=1, si_search_ratio=2),
+    dict(si_skew_stream=1, si_stage_bytes=1024, si_stage_slots=3),
 ])
 def test_batched_schedules_agree(ctx, cfg):
     """Small staging slots cut most pairs into many chunk pairs; results must not change."""
@@ -224,4 +227,42 @@ def test_bounded_wait_runs_out_cleanly(ctx):
     for _ in range(2):  # the hook applied to one launch only; the context stays usable
         got, _ = sets.count(pa, pb, rtg.SI_AUTO)
         assert np.array_equal(got, exp)
+    sets.close()
+
+
+def test_skewed_pairs_streamed_match_oracle(ctx):
+    """Skewed pairs longer than a staging slot, every alignment of the long list and short
+    lists from 1 to 128 elements: the staged-and-streamed form (si_skew_stream) against the
+    oracle, and against the searched form."""
+    rng = np.random.default_rng(21)
+    lens = []
+    for a in (1, 2, 3, 5, 17, 31, 32, 33, 64, 100, 127, 128):
+        for b in (1100, 1101, 1102, 1103, 2000, 4097):
+            lens += [a, b]
+    off = np.zeros(len(lens) + 1, np.uint64)
+    off[1:] = np.cumsum(lens)
+    el = np.empty(int(off[-1]), np.uint32)
+    for i in range(0, len(lens), 2):
+        a, b = lens[i], lens[i + 1]
+        B = np.sort(rng.choice(1 << 24, size=b, replace=False)).astype(np.uint32)
+        k = int(rng.integers(0, a + 1))
+        A = np.concatenate([rng.choice(B, size=k, replace=False),
+                            rng.choice(np.setdiff1d(np.arange(1 << 24, (1 << 24) + 4 * a), B),
+                                       size=a - k, replace=False)])
+        el[off[i]:off[i + 1]] = np.sort(A)
+        el[off[i + 1]:off[i + 2]] = B
+    pa = np.arange(0, len(lens), 2, dtype=np.uint32)
+    pb = pa + 1
+    sets = ctx.sets(off, el)
+    want = oracle.si_pairs(off, el, pa, pb)
+    saved = ctx.config().as_dict()
+    try:
+        for stream in (0, 1):
+            ctx.set_config(**dict(saved, si_skew_stream=stream))
+            got, _ = sets.count(pa, pb, rtg.SI_AUTO)
+            assert np.array_equal(got, want), stream
+            got, _ = sets.count(pb, pa, rtg.SI_AUTO)
+            assert np.array_equal(got, want), stream
+    finally:
+        ctx.set_config(**saved)
     sets.close()

@@ -35,7 +35,7 @@ def test_tune_si_keeps_exact_counts_and_caches(tmp_path):
     with rtg.Context(0) as ctx:
         sets = ctx.sets(off, el)
         r = sets.tune(pa, pb, cache)
-        assert not r["from_cache"] and r["candidates"] == 108
+        assert not r["from_cache"] and r["candidates"] == 109
         assert r["best_ms"] <= r["default_ms"]
         got, _ = sets.count(pa, pb, rtg.SI_AUTO)
         assert np.array_equal(got, exp)
