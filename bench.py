@@ -662,6 +662,17 @@ def run_gpu(args, dist: Dist) -> None:
             raise RuntimeError("plain count differs from batched count")
         plain_ms.append(t2.count_ms)
     plain_value, _ = aggregate(dist, m, sum(plain_ms) / len(plain_ms))
+    # ---- the counting-form kernel without persistence, graph or tuning (one launch per
+    # item bucket, items built on every call): separates algorithm from scheduling
+    buck_ms, buck_kms = [], []
+    for _ in range(args.steps):
+        ctx.flush_l2()
+        tb, t3 = g.tc(rtg.TC_BUCKETED)
+        if tb != want:
+            raise RuntimeError("bucketed count differs from batched count")
+        buck_ms.append(t3.count_ms)
+        buck_kms.append(t3.main_kernel_ms)
+    buck_value, _ = aggregate(dist, m, sum(buck_ms) / len(buck_ms))
     # ---- end to end through the C ABI with pinned host buffers
     hs = ctx.host_array(len(s), np.uint32)
     hd = ctx.host_array(len(d), np.uint32)
@@ -748,6 +759,14 @@ def run_gpu(args, dist: Dist) -> None:
                 "plain": {"value": plain_value, "unit": UNIT,
                           "ms_per_step": sum(plain_ms) / len(plain_ms)},
                 "batched_over_plain": value / plain_value,
+                "bucketed": {"value": buck_value, "unit": UNIT,
+                             "ms_per_step": sum(buck_ms) / len(buck_ms),
+                             "kernel_ms": sum(buck_kms) / len(buck_kms),
+                             "form": "the batched kernel's algorithm (counting form, suffix "
+                                     "streaming) launched once per item bucket, no persistence, "
+                                     "no CUDA graph, default schedule, items built every call"},
+                "bucketed_over_plain": buck_value / plain_value,
+                "batched_over_bucketed": value / buck_value,
                 "roofline": roofline, "cpu_baseline": cpu, "clocks": clk.summary(),
                 "gpu_launches": int(launches), "schedule": tune, "si": si,
                 "serving": serving}

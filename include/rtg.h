@@ -93,7 +93,13 @@ typedef enum rtg_orient {
  *  BATCHED : persistent kernel over a device work queue of (vertex, edge-range) items,
  *            out-list of the source vertex staged in shared memory, launched as one
  *            CUDA graph, schedule from the context configuration (autotuned). */
-typedef enum rtg_tc_mode { RTG_TC_PLAIN = 0, RTG_TC_BATCHED = 1 } rtg_tc_mode;
+/* Triangle-count forms. PLAIN: the reference's per-edge formulation (one warp per oriented
+ * edge, one launch per degree/ratio bucket). BATCHED: the counting form streamed by the
+ * persistent kernel from a device queue, replayed from a CUDA graph, autotunable.
+ * BUCKETED: the same counting-form kernel without persistence or graph: work items built
+ * on every call, one launch per item-size bucket with one warp per item, the library's
+ * default schedule (it separates what the algorithm and what the scheduling contribute). */
+typedef enum rtg_tc_mode { RTG_TC_PLAIN = 0, RTG_TC_BATCHED = 1, RTG_TC_BUCKETED = 2 } rtg_tc_mode;
 
 /* Set-intersection execution forms (flags of rtg_si_count*).
  *  AUTO   : BATCHED form — one persistent launch; both lists of every pair (or of every

@@ -339,7 +339,8 @@ rtg_status rtg_csr_build(rtg_ctx *ctx, rtg_graph *g, rtg_orient orient) {
         cudaStreamSynchronize(ctx->stream);
         tc_plan_free(g->plan_batched);
         tc_plan_free(g->plan_plain);
-        g->plan_batched = g->plan_plain = nullptr;
+        tc_plan_free(g->plan_bucketed);
+        g->plan_batched = g->plan_plain = g->plan_bucketed = nullptr;
         count_csr_free(g->cnt);
     }
     RTG_TRY(build_csr(ctx, g, orient));
@@ -419,6 +420,7 @@ void rtg_graph_destroy(rtg_graph *g) {
     }
     tc_plan_free(g->plan_batched);
     tc_plan_free(g->plan_plain);
+    tc_plan_free(g->plan_bucketed);
     dev_free(g->d_src);
     dev_free(g->d_dst);
     graph_free_csr(g->ori);
@@ -545,7 +547,7 @@ rtg_status rtg_graph_from_host_csr(rtg_ctx *ctx, const int32_t *offsets, const i
 rtg_status rtg_tc_count(rtg_ctx *ctx, rtg_graph *g, rtg_tc_mode mode, uint64_t *out_total,
                         rtg_timing *timing) {
     if (!ctx || !g || !out_total) return RTG_ERR_INVALID_ARG;
-    if (mode != RTG_TC_PLAIN && mode != RTG_TC_BATCHED)
+    if (mode != RTG_TC_PLAIN && mode != RTG_TC_BATCHED && mode != RTG_TC_BUCKETED)
         return fail(ctx, RTG_ERR_INVALID_ARG, "unknown tc mode %d", (int)mode);
     if (!g->ori.built) return fail(ctx, RTG_ERR_STATE, "oriented CSR not built");
     rtg_timing t{};

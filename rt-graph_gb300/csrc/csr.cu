@@ -642,7 +642,8 @@ rtg_status build_count_direct(rtg_ctx *ctx, rtg_graph *g, bool in_scratch, bool 
     const uint64_t m = g->m_input;
     tc_plan_free(g->plan_batched);
     tc_plan_free(g->plan_plain);
-    g->plan_batched = g->plan_plain = nullptr;
+    tc_plan_free(g->plan_bucketed);
+    g->plan_batched = g->plan_plain = g->plan_bucketed = nullptr;
     uint32_t maxid = 0;
     if (pre && raw_degree) {
         maxid = pre->maxid;

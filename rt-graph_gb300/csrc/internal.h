@@ -105,6 +105,7 @@ struct rtg_graph {
     rtg::Csr sym;               // symmetric CSR
     rtg::TcPlan *plan_batched = nullptr;
     rtg::TcPlan *plan_plain = nullptr;
+    rtg::TcPlan *plan_bucketed = nullptr;
 };
 
 struct rtg_sets {

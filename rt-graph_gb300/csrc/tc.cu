@@ -185,10 +185,31 @@ __global__ void k_item_fill(const uint64_t *__restrict__ off, const uint64_t *__
     if (blockIdx.x == 0 && threadIdx.x == 0) acc[2] = base[n];
 }
 
+// BUCKETED form: the items sorted by the in-edges they hold (at most 32, at most 256, more)
+// into kItemBuckets regions of cap entries; cnt[r] counts region r.
+constexpr int kItemBuckets = 3;
+
+__global__ void k_item_bucket(const uint64_t *__restrict__ items,
+                              const unsigned long long *__restrict__ nitems,
+                              const uint64_t *__restrict__ in_off, uint32_t E, uint64_t cap,
+                              uint64_t *out, unsigned long long *cnt) {
+    const unsigned long long ni = *nitems;
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < ni;
+         i += (uint64_t)gridDim.x * blockDim.x) {
+        const uint64_t it = items[i];
+        const uint32_t v = (uint32_t)(it >> 32), k0 = (uint32_t)it;
+        const uint32_t ne = min(E, (uint32_t)(in_off[v + 1] - in_off[v]) - k0);
+        const int r = ne <= 32 ? 0 : (ne <= 256 ? 1 : 2);
+        out[r * cap + atomicAdd(&cnt[r], 1ull)] = it;
+    }
+}
+
 struct WarpCfg {
     uint32_t E;      // in-edges per item
     uint32_t R;      // 32-bit words of the per-warp shared-memory region (bitmap or table)
     uint32_t n;      // vertices of the counting form
+    uint32_t first;  // one-item-per-warp launches: the items [first, last) of `items`
+    uint32_t last;
 };
 
 // 1 << s for s < 32, 0 for s >= 32 (PTX clamps the shift amount; C++ leaves it undefined)
@@ -351,6 +372,10 @@ __host__ __device__ constexpr uint32_t region_words(uint32_t R) {
 // every element is a rank above v >= 0). A suffix element w is tested in the bitmap when
 // w >= W0, else in the table. An out-list with more than kLowHashWords / 2 elements below
 // the window (none on R-MAT or Holme-Kim graphs) is merged against each suffix instead.
+//
+// kPersistent: warps take items from the queue (acc[1]) until acc[2] items are done;
+// otherwise warp w of the grid takes item first + w only (one launch per item bucket).
+template <bool kPersistent>
 __global__ void __maxnreg__(48) k_tc_warp(const uint64_t *__restrict__ off, const uint32_t *__restrict__ adj,
                           const uint64_t *__restrict__ in_off, const uint2 *__restrict__ in_rng,
                           const uint64_t *__restrict__ items, unsigned long long *acc,
@@ -371,9 +396,14 @@ __global__ void __maxnreg__(48) k_tc_warp(const uint64_t *__restrict__ off, cons
     unsigned long long cnt = 0;
     while (true) {
         unsigned long long k = 0;
-        if (lane == 0) k = atomicAdd(&acc[1], 1ull);
-        k = __shfl_sync(kFull, k, 0);
-        if (k >= nitems) break;
+        if (kPersistent) {
+            if (lane == 0) k = atomicAdd(&acc[1], 1ull);
+            k = __shfl_sync(kFull, k, 0);
+            if (k >= nitems) break;
+        } else {
+            k = p.first + (unsigned long long)blockIdx.x * (blockDim.x >> 5) + warp;
+            if (k >= p.last) break;
+        }
         const uint64_t it = items[k];
         const uint32_t v = (uint32_t)(it >> 32), k0 = (uint32_t)it;
         const uint64_t ov = off[v];
@@ -441,6 +471,7 @@ __global__ void __maxnreg__(48) k_tc_warp(const uint64_t *__restrict__ off, cons
                 for (uint32_t q = lane; q < kLowHashWords; q += 32) tab[q] = 0u;
         }
         __syncwarp();
+        if (!kPersistent) break;
     }
     block_add_total(cnt, &acc[0], red);
 }
@@ -462,6 +493,8 @@ struct TcPlan {
     // plain
     uint8_t *bucket = nullptr;
     uint32_t *lists = nullptr;
+    // bucketed: items sorted into kItemBuckets regions of item_cap entries each
+    uint64_t *bitems = nullptr;
     cudaEvent_t bev[2 * kPlainBuckets] = {};
 };
 
@@ -475,6 +508,7 @@ void tc_plan_free(TcPlan *p) {
     dev_free(p->acc);
     dev_free(p->bucket);
     dev_free(p->lists);
+    dev_free(p->bitems);
     if (p->k0) cudaEventDestroy(p->k0);
     if (p->k1) cudaEventDestroy(p->k1);
     for (auto ev : p->bev)
@@ -527,10 +561,10 @@ rtg_status batched_shape(rtg_ctx *ctx, const CountCsr &c, const rtg_config &cfg,
     RTG_CUDA(ctx, cub::DeviceScan::ExclusiveSum(nullptr, bs->cub_bytes, (uint32_t *)nullptr,
                                                 (uint32_t *)nullptr, (int64_t)c.n + 1,
                                                 ctx->stream));
-    RTG_CUDA(ctx, cudaFuncSetAttribute(k_tc_warp, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    RTG_CUDA(ctx, cudaFuncSetAttribute(k_tc_warp<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        (int)bs->smem));
     int per_sm = 0;
-    RTG_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_tc_warp, bs->W * 32,
+    RTG_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_tc_warp<true>, bs->W * 32,
                                                                 bs->smem));
     if (cfg.tc_blocks_per_sm) per_sm = std::min<int>(per_sm, (int)cfg.tc_blocks_per_sm);
     per_sm = std::max(per_sm, 1);
@@ -561,7 +595,7 @@ void enqueue_count(cudaStream_t st, const CountCsr &c, const BatchedShape &bs,
         if (external_events) cudaEventRecordWithFlags(k0, st, cudaEventRecordExternal);
         else cudaEventRecord(k0, st);
     }
-    k_tc_warp<<<bs.grid, bs.W * 32, bs.smem, st>>>(c.off, c.adj, c.in_off, c.in_rng, items, acc,
+    k_tc_warp<true><<<bs.grid, bs.W * 32, bs.smem, st>>>(c.off, c.adj, c.in_off, c.in_rng, items, acc,
                                                    bs.pc);
     if (k1) {
         if (external_events) cudaEventRecordWithFlags(k1, st, cudaEventRecordExternal);
@@ -752,6 +786,83 @@ rtg_status count_plain(rtg_ctx *ctx, rtg_graph *g, uint64_t *total, rtg_timing *
     return RTG_OK;
 }
 
+// The counting-form kernel without persistence or graph, with the library's default
+// schedule: work items built on every call, sorted into size buckets, one launch per
+// non-empty bucket with one warp per item (grid = items / warps per block).
+rtg_status count_bucketed(rtg_ctx *ctx, rtg_graph *g, uint64_t *total, rtg_timing *t) {
+    const CountCsr &c = g->cnt;
+    if (!c.built) return fail(ctx, RTG_ERR_STATE, "counting form of the CSR is missing");
+    rtg_config dcfg{};
+    dcfg.tc_item_edges = c.m >= kLargeItemsFrom ? kLargeItemEdges : kDefaultItemEdges;
+    dcfg.tc_block_warps = kDefaultBlockWarps;
+    dcfg.tc_region_words = kDefaultRegionWords;
+    BatchedShape bs{};
+    RTG_TRY(batched_shape(ctx, c, dcfg, &bs));
+    TcPlan *p = g->plan_bucketed;
+    if (!p) {
+        p = new TcPlan();
+        p->mode = RTG_TC_BUCKETED;
+        rtg_status s = dev_alloc(ctx, (void **)&p->items, bs.item_cap * 8);
+        if (s == RTG_OK) s = dev_alloc(ctx, (void **)&p->bitems, bs.item_cap * 8 * kItemBuckets);
+        if (s == RTG_OK) s = dev_alloc(ctx, (void **)&p->vcnt, (c.n + 1ull) * 4 * 2);
+        if (s == RTG_OK) s = dev_alloc(ctx, (void **)&p->acc, 8 * sizeof(unsigned long long));
+        if (s == RTG_OK) s = dev_alloc(ctx, &p->cub_tmp, bs.cub_bytes);
+        if (s != RTG_OK) {
+            tc_plan_free(p);
+            return s;
+        }
+        g->plan_bucketed = p;
+    }
+    RTG_CUDA(ctx, cudaFuncSetAttribute(k_tc_warp<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)bs.smem));
+    const uint64_t l0 = ctx->launches;
+    unsigned long long *acc = p->acc, *bcnt = p->acc + 3;
+    RTG_CUDA(ctx, cudaEventRecord(ctx->ev[0], ctx->stream));
+    enqueue_items(ctx->stream, c, bs, p->items, p->vcnt, p->cub_tmp, acc);  // zeroes acc[0..7]
+    ctx->launches += kBatchedKernels - 1;
+    const int gb = (int)std::max<uint64_t>(1, std::min<uint64_t>((bs.item_cap + 255) / 256,
+                                                                  ctx->sm_count * 16ull));
+    k_item_bucket<<<gb, 256, 0, ctx->stream>>>(p->items, acc + 2, c.in_off, bs.pc.E, bs.item_cap,
+                                               p->bitems, bcnt);
+    ctx->launches++;
+    RTG_CUDA(ctx, cudaGetLastError());
+    unsigned long long hc[kItemBuckets] = {0};
+    RTG_CUDA(ctx, cudaMemcpyAsync(hc, bcnt, sizeof hc, cudaMemcpyDeviceToHost, ctx->stream));
+    RTG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    float kms_sum = 0;
+    for (int r = 0; r < kItemBuckets; ++r) {
+        if (!hc[r]) continue;
+        WarpCfg pc = bs.pc;
+        pc.first = 0;
+        pc.last = (uint32_t)hc[r];
+        const uint64_t blocks = (hc[r] + bs.W - 1) / bs.W;
+        RTG_CUDA(ctx, cudaEventRecord(ctx->ev[4], ctx->stream));
+        k_tc_warp<false><<<(unsigned)blocks, bs.W * 32, bs.smem, ctx->stream>>>(
+            c.off, c.adj, c.in_off, c.in_rng, p->bitems + r * bs.item_cap, acc, pc);
+        ctx->launches++;
+        RTG_CUDA(ctx, cudaGetLastError());
+        RTG_CUDA(ctx, cudaEventRecord(ctx->ev[5], ctx->stream));
+        RTG_CUDA(ctx, cudaEventSynchronize(ctx->ev[5]));
+        float ms = 0;
+        cudaEventElapsedTime(&ms, ctx->ev[4], ctx->ev[5]);
+        kms_sum += ms;
+    }
+    RTG_CUDA(ctx, cudaEventRecord(ctx->ev[1], ctx->stream));
+    unsigned long long h = 0;
+    RTG_CUDA(ctx, cudaMemcpyAsync(&h, acc, 8, cudaMemcpyDeviceToHost, ctx->stream));
+    RTG_CUDA(ctx, cudaEventRecord(ctx->ev[2], ctx->stream));
+    RTG_CUDA(ctx, cudaEventSynchronize(ctx->ev[2]));
+    *total = h;
+    float ms = 0, dms = 0;
+    cudaEventElapsedTime(&ms, ctx->ev[0], ctx->ev[1]);
+    cudaEventElapsedTime(&dms, ctx->ev[1], ctx->ev[2]);
+    t->count_ms = ms;
+    t->main_kernel_ms = kms_sum;
+    t->d2h_ms += dms;
+    t->kernel_launches += ctx->launches - l0;
+    return RTG_OK;
+}
+
 }  // namespace
 
 uint64_t tc_plan_estimate_bytes(const rtg_ctx *ctx, const rtg_graph *g) {
@@ -824,6 +935,7 @@ rtg_status tc_count(rtg_ctx *ctx, rtg_graph *g, rtg_tc_mode mode, uint64_t *tota
         return RTG_OK;
     }
     if (mode == RTG_TC_PLAIN) return count_plain(ctx, g, total, t);
+    if (mode == RTG_TC_BUCKETED) return count_bucketed(ctx, g, total, t);
     return count_batched(ctx, g, total, t);
 }
 

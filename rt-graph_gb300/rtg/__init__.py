@@ -26,7 +26,7 @@ OK, ERR_INVALID_ARG, ERR_OOM, ERR_IO, ERR_FORMAT, ERR_DEVICE, ERR_TIMEOUT, ERR_C
     ERR_STATE, ERR_BUSY = range(10)
 FMT_EDGE_BIN, FMT_EDGE_TXT, FMT_MTX, FMT_RTG_CSR = 0, 1, 2, 3
 ORIENT_DEGREE, ORIENT_DEGREE_RAW_REF, ORIENT_SYMMETRIC = 0, 1, 2
-TC_PLAIN, TC_BATCHED = 0, 1
+TC_PLAIN, TC_BATCHED, TC_BUCKETED = 0, 1, 2
 SI_AUTO, SI_MERGE, SI_SEARCH, SI_BITMAP, SI_PLAIN = 0, 1, 2, 3, 4
 PAIRS_DEVICE, OUT_DEVICE = 0x100, 0x200
 

@@ -17,7 +17,7 @@ from conftest import golden_edges, sha_i32, tc_golden
 
 pytestmark = pytest.mark.gpu
 TC = tc_golden()
-MODES = (rtg.TC_PLAIN, rtg.TC_BATCHED)
+MODES = (rtg.TC_PLAIN, rtg.TC_BATCHED, rtg.TC_BUCKETED)
 
 
 @pytest.mark.parametrize("name", sorted(TC))
