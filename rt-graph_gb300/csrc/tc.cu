@@ -225,7 +225,7 @@ __device__ __forceinline__ uint32_t bit_or_zero(uint32_t s) {
 // after j: one ballot, one popcount and one shuffle per unit, no branch per in-edge. Each
 // unit is S coalesced 32-bit loads per lane; kUnitDepth units are in flight ahead of the one
 // being tested (units past the last hold idle elements).
-constexpr int kUnitDepth = 3;
+constexpr int kUnitDepth = 2;
 
 template <int S, class F>
 __device__ __forceinline__ uint32_t stream_units(const uint32_t *__restrict__ adjl, uint32_t nu,
