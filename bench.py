@@ -29,10 +29,12 @@ oriented by degree. A step is one exact uint64 count of the resident CSR:
             alone as a full line (with its CPU baseline).
 
 `--impl reference` times the reference's counting logic on the host cores: the oracle's
-restatement of ListIntersectionKernel (the reference's own sources are not present on the
-benchmark host, and its GPU formulations need OptiX or are the same per-edge algorithm),
-on a stride sample of the same workload, which it generates with the oracle's copy of the
-seeded generator, so that the library under test is not loaded in that process.
+restatement of ListIntersectionKernel, on a stride sample of the same workload, which it
+generates with the oracle's copy of the seeded generator, so that the library under test is
+not loaded in that process. Beside it (`reference_gpu`) it times the reference's own GPU
+kernel for the same count (ListIntersectionKernel, its method 0, compiled unmodified from
+its sources by oracle/build_ref.sh into a cubin, launched through the CUDA driver API by
+oracle/ref_gpu.py), when that cubin was built.
 With torchrun (N>1) every rank runs an independent replica on its own GPU (the count does
 not shard across GPUs here); rank 0 prints one line with the max time over ranks.
 """
@@ -613,8 +615,28 @@ def run_reference(args, dist: Dist) -> None:
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
                              "sample": sample},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0,
-                    "d2h_bytes_per_step": 0}}
+                    "d2h_bytes_per_step": 0},
+            "reference_gpu": reference_gpu_point(off, adj, m, args)}
     print(json.dumps(line), flush=True)
+
+
+def reference_gpu_point(off: np.ndarray, adj: np.ndarray, m: int, args) -> dict:
+    """The reference's own GPU count on the same oriented CSR, beside the CPU arm: its
+    ListIntersectionKernel (tc/bs_tc/bs_tc.cu:120-148, method 0, compiled unmodified by
+    oracle/build_ref.sh where the reference's sources are) launched as its CountOnGPU does,
+    timed with CUDA events; its count is checked against the oracle's merge counter."""
+    from oracle import ref_gpu
+    ok, why = ref_gpu.available()
+    if not ok:
+        return {"unavailable": why}
+    import oracle
+    total, times = ref_gpu.count(off, adj, runs=max(1, min(args.steps, 5)))
+    ms = sum(times) / len(times)
+    return {"value": m / (ms / 1e3), "unit": UNIT, "ms_per_step": ms, "steps": len(times),
+            "triangles": total, "exact": total == oracle.tc_merge(off, adj),
+            "kernel": "ListIntersectionKernel (tc/bs_tc/bs_tc.cu:120-148), the reference's "
+                      "method 0, 256 threads per block, at most 65,535 blocks, uint32 counter",
+            "timing": "CUDA events around each launch, kernel only (CSR resident)"}
 
 
 def run_gpu(args, dist: Dist) -> None:

@@ -9,7 +9,8 @@
 # Without REF the checkout is looked up next to this repository (../reference).
 #
 # Reference files used (read-only): tc/graph/graph.cpp, tc/bs_tc/bs_tc.cu (its host
-# function Preprocessing; the kernels in the same file compile but never run),
+# function Preprocessing for the driver; its method-0 kernel ListIntersectionKernel as a
+# cubin for the benchmark's reference GPU data point, oracle/ref_gpu.py),
 # set_intersection/data_generator/data.cpp. ThrustSortEdgesInBatch is provided on the
 # host by oracle/ref_shim.cpp. CCCL 3 no longer pulls <vector>, <algorithm> and <cassert>
 # into bs_tc.cu, so they are force-included.
@@ -30,6 +31,11 @@ nvcc -O2 -std=c++17 -Xcompiler -fopenmp -include vector -include algorithm -incl
   $INC -gencode arch=compute_103a,code=sm_103a -c "$REF/tc/bs_tc/bs_tc.cu" -o "$OUT/bs_tc.o" &
 g++ -O2 -std=c++17 $INC -c "$HERE/ref_shim.cpp" -o "$OUT/ref_shim.o" &
 g++ -O2 -std=c++17 $INC -c "$HERE/ref_driver.cpp" -o "$OUT/ref_driver.o" &
+# the reference's own GPU triangle count, method 0 (ListIntersectionKernel), device code
+# only: loaded and launched by oracle/ref_gpu.py through the CUDA driver API
+nvcc -O3 -std=c++17 -cubin -gencode arch=compute_103a,code=sm_103a -include "$HERE/ref_method0.h" \
+  -include vector -include algorithm -include cassert $INC -I"$REF/tc/rt_tc/include" \
+  "$REF/tc/bs_tc/bs_tc.cu" -o "$OUT/bs_tc_method0.cubin" &
 wait
 g++ -fopenmp -o "$OUT/ref_driver" "$OUT/ref_driver.o" "$OUT/ref_shim.o" "$OUT/graph.o" \
   "$OUT/bs_tc.o" "$OUT/data.o" -L"$CUDA_HOME/lib64" -lcudart
