@@ -70,7 +70,7 @@ def _stale(target: Path, deps: list[Path]) -> bool:
 
 def _headers() -> list[Path]:
     return sorted(list(INCLUDE.glob("*.h")) + list(CSRC.glob("*.h")) + list(CSRC.glob("*.cuh"))
-                  + list(HOST.glob("*.h")))
+                  + list(HOST.glob("*.h")) + list(CLI.glob("*.h")))
 
 
 def _compile(src: Path, obj: Path) -> Path:

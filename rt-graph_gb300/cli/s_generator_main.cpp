@@ -21,6 +21,7 @@
 #include <vector>
 
 #include "args.h"
+#include "gen_sets.h"
 
 namespace {
 
@@ -92,29 +93,9 @@ int main(int argc, char *argv[]) {
         return (uint32_t)std::round(range * v);
     };
 
-    std::vector<uint32_t> a(len_a);
-    std::unordered_set<uint32_t> in_a;
-    for (uint32_t i = 0; i < len_a; ++i) {
-        uint32_t x;
-        do x = draw_a();
-        while (in_a.count(x));
-        in_a.insert(x);
-        a[i] = x;
-    }
-    std::sort(a.begin(), a.end());
-    std::vector<std::vector<uint32_t>> bs(num_b, std::vector<uint32_t>(len_b));
-    for (auto &b : bs) {
-        std::copy(a.begin(), a.begin() + len_c, b.begin());
-        std::unordered_set<uint32_t> used = in_a;
-        for (uint32_t j = len_c; j < len_b; ++j) {
-            uint32_t x;
-            do x = draw_b();
-            while (used.count(x));
-            used.insert(x);
-            b[j] = x;
-        }
-        std::sort(b.begin(), b.end());
-    }
+    std::vector<uint32_t> a;
+    std::vector<std::vector<uint32_t>> bs;
+    build_sets(len_a, len_b, len_c, num_b, draw_a, draw_b, a, bs);
 
     std::string name;
     if (lambda > 0)
@@ -124,21 +105,10 @@ int main(int argc, char *argv[]) {
         name = std::to_string(len_a) + "_" + std::to_string(len_b) + "_" + std::to_string(len_c) +
                "_" + std::to_string(range) + ".s_data";
     const std::string path = dir + name;
-    std::ofstream f(path, std::ios::binary);
-    if (!f) {
+    if (!write_sets_file(path, num_a, range, len_c, a, bs)) {
         std::cerr << "File error" << std::endl;
         return 1;
     }
-    const uint32_t header[4] = {num_a, num_b, range, len_c};
-    f.write(reinterpret_cast<const char *>(header), sizeof header);
-    uint32_t off = 0;
-    for (uint32_t i = 0; i < num_a + num_b; ++i) {
-        f.write(reinterpret_cast<const char *>(&off), 4);
-        off += (i < num_a) ? len_a : len_b;
-    }
-    f.write(reinterpret_cast<const char *>(&off), 4);
-    for (uint32_t i = 0; i < num_a; ++i) f.write(reinterpret_cast<const char *>(a.data()), 4ull * len_a);
-    for (auto &b : bs) f.write(reinterpret_cast<const char *>(b.data()), 4ull * len_b);
     std::cout << "Data: length of set A = " << len_a << ", length of set B = " << len_b
               << ", length of set C = " << len_c << ", element range = " << range << std::endl;
     std::cout << "Data has been written to path: " << path << std::endl;
