@@ -397,6 +397,11 @@ def measure_si(args, dist: Dist, ctx, cpu: bool) -> dict:
     kms = sum(kms_steps) / len(kms_steps)
     peaks = measured_peaks()
     achieved = algo / (kms / 1e3) / 1e9
+    # the kernel of the batched form the context ran (si_form 0 is the library default, the
+    # producer/consumer form) and its committed ncu summary
+    pc_form = tuned.get("si_form", 0) in (0, 2)
+    kernel = "k_si_pc" if pc_form else "k_si_stream"
+    prof = "si_pc_lognormal_1e6" if pc_form else "si_stream_lognormal_1e6"
     res = {
         "value": value, "unit": SI_UNIT, "ms_per_step": ms, "launches": int(launches),
         "config": dict(SI_WORKLOAD, mode="batched (persistent staged kernel)",
@@ -409,10 +414,10 @@ def measure_si(args, dist: Dist, ctx, cpu: bool) -> dict:
                 "api": "rtg_si_count (pinned host pair ids and counts, sets resident)"},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peaks["hbm_gbs"],
                      "unit": "GB/s", "frac": achieved / peaks["hbm_gbs"],
-                     "traffic": profile_traffic("si_stream_lognormal_1e6"),
-                     "peak_source": peaks["source"], "kernel": "k_si_stream", "kernel_ms": kms,
+                     "traffic": profile_traffic(prof),
+                     "peak_source": peaks["source"], "kernel": kernel, "kernel_ms": kms,
                      "algo_bytes_per_launch": algo,
-                     **dram_view(profile_traffic("si_stream_lognormal_1e6"), kms,
+                     **dram_view(profile_traffic(prof), kms,
                                  peaks["hbm_gbs"], "pairs longer than a slot with |B| > 8 |A| "
                                  "are searched in global memory, not streamed")},
         "clocks": clk.summary(),

@@ -36,7 +36,7 @@
 extern "C" {
 #endif
 
-#define RTG_ABI_VERSION 2
+#define RTG_ABI_VERSION 3
 
 /* Status codes. The reference prints and calls exit(2) on any CUDA error
  * (tc/utils/common.h:13-32); librtg returns one of these instead. */
@@ -104,9 +104,10 @@ typedef enum rtg_tc_mode { RTG_TC_PLAIN = 0, RTG_TC_BATCHED = 1, RTG_TC_BUCKETED
 /* Set-intersection execution forms (flags of rtg_si_count*).
  *  AUTO   : BATCHED form — one persistent launch; both lists of every pair (or of every
  *           chunk pair of a long pair) are staged into shared memory by bulk copies and
- *           merged there, several pairs in flight per warp; a pair longer than a staging
- *           slot whose long list exceeds si_search_ratio (default 8) x the short one is
- *           binary-searched from global memory instead.
+ *           merged there; by default one warp per block forms the jobs and issues their
+ *           copies into a ring of slots that the block's other warps merge (si_form); a
+ *           pair longer than a staging slot whose long list exceeds si_search_ratio
+ *           (default 8) x the short one is binary-searched from global memory instead.
  *  PLAIN  : per-pair family from global memory: SEARCH when |long| > si_search_ratio
  *           (default 32) x |short|, MERGE otherwise.
  *  FORCE_*: one family for every pair; these back the reference's per-baseline CLIs. */
@@ -161,7 +162,8 @@ typedef struct rtg_config {
     uint32_t si_block_warps;    /* warps per block of the SI kernels                  */
     uint32_t si_search_ratio;   /* long/short length ratio above which the forced-
                                    family-free PLAIN form uses SEARCH                 */
-    uint32_t si_stage_slots;    /* bulk-copy staging slots per warp (2..16)           */
+    uint32_t si_stage_slots;    /* bulk-copy staging slots per warp, or per block in the
+                                   producer/consumer form (2..32)                     */
     uint32_t si_stage_bytes;    /* bytes per staging slot (multiple of 128, 512..32768) */
     uint32_t si_blocks_per_sm;  /* resident blocks per SM of the batched SI kernel    */
     uint32_t si_skew_stream;    /* 1: a skewed pair longer than a staging slot whose short
@@ -169,6 +171,12 @@ typedef struct rtg_config {
                                    list in shared memory (bulk copy) and streaming the long
                                    list from HBM in 16-byte loads, when that reads fewer
                                    sectors than searching it; 0 (default): always searched */
+    uint32_t si_form;           /* batched SI kernel form: 1 = every warp forms its own jobs
+                                   and merges them (si_stage_slots slots per warp); 2 =
+                                   producer/consumer: one warp per block forms the jobs and
+                                   issues their bulk copies into a ring of si_stage_slots
+                                   slots shared by si_block_warps merging warps; 0 = library
+                                   default                                            */
 } rtg_config;
 
 /* ---------------------------------------------------------------- context */
@@ -349,7 +357,7 @@ rtg_status rtg_si_materialize(rtg_ctx *ctx, const rtg_sets *s, const uint32_t *p
  * Time a grid of schedules for the batched forms (after an L2 flush, median of three
  * runs each), keep the fastest whose result is bit-identical to the default schedule's,
  * and set it on the context. TC: tc_item_edges x tc_region_words x tc_block_warps. SI:
- * si_stage_bytes x si_stage_slots x si_block_warps x si_search_ratio, on the pairs given
+ * si_form x si_stage_bytes x si_stage_slots x si_block_warps x si_search_ratio, on the pairs given
  * (host arrays; a representative sample of the workload). With cache_path (a text file,
  * created if missing) the winner is stored under a key of the device and the workload's
  * size class, and a later call with the same key applies it without searching. */

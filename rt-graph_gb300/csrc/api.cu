@@ -167,8 +167,10 @@ void rtg_destroy(rtg_ctx *ctx) {
     for (auto &b : ctx->scratch) dev_free(b.ptr);
     for (auto &b : ctx->work) dev_free(b.ptr);
     dev_free(ctx->flush_buf);
-    if (ctx->si_exec) cudaGraphExecDestroy(ctx->si_exec);
-    if (ctx->si_graph) cudaGraphDestroy(ctx->si_graph);
+    for (auto &kg : ctx->si_graphs) {
+        if (kg.exec) cudaGraphExecDestroy(kg.exec);
+        if (kg.graph) cudaGraphDestroy(kg.graph);
+    }
     dev_free(ctx->d_status);
     dev_free(ctx->d_scalars);
     for (auto &ev : ctx->ev)
@@ -185,14 +187,16 @@ rtg_status rtg_set_config(rtg_ctx *ctx, const rtg_config *cfg) {
         return fail(ctx, RTG_ERR_INVALID_ARG, "tc_region_words must be in [64, 16384]");
     if (cfg->tc_block_warps > 32 || cfg->si_block_warps > 32)
         return fail(ctx, RTG_ERR_INVALID_ARG, "at most 32 warps per block");
-    if (cfg->si_stage_slots && (cfg->si_stage_slots < 2 || cfg->si_stage_slots > 16))
-        return fail(ctx, RTG_ERR_INVALID_ARG, "si_stage_slots must be in [2, 16]");
+    if (cfg->si_stage_slots && (cfg->si_stage_slots < 2 || cfg->si_stage_slots > 32))
+        return fail(ctx, RTG_ERR_INVALID_ARG, "si_stage_slots must be in [2, 32]");
     if (cfg->si_stage_bytes && (cfg->si_stage_bytes < 512 || cfg->si_stage_bytes % 128 ||
                                 cfg->si_stage_bytes > 32768))
         return fail(ctx, RTG_ERR_INVALID_ARG,
                     "si_stage_bytes must be a multiple of 128 in [512, 32768]");
     if (cfg->si_skew_stream > 1)
         return fail(ctx, RTG_ERR_INVALID_ARG, "si_skew_stream must be 0 or 1");
+    if (cfg->si_form > 2)
+        return fail(ctx, RTG_ERR_INVALID_ARG, "si_form must be 0, 1 or 2");
     ctx->cfg = *cfg;
     return RTG_OK;
 }

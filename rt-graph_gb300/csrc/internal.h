@@ -68,11 +68,14 @@ struct rtg_ctx {
     std::string last_error;
     rtg_config cfg{};
     uint64_t launches = 0;
-    // the batched SI launch (queue-head reset + persistent kernel) as a CUDA graph, captured
-    // on the first launch; later launches update the kernel node's parameters and replay it
-    cudaGraph_t si_graph = nullptr;
-    cudaGraphExec_t si_exec = nullptr;
-    cudaGraphNode_t si_knode = nullptr;
+    // the batched SI launch (queue-head reset + persistent kernel) as a CUDA graph per kernel
+    // form, captured on the first launch; later launches update the kernel node's
+    // parameters and replay it
+    struct KernelGraph {
+        cudaGraph_t graph = nullptr;
+        cudaGraphExec_t exec = nullptr;
+        cudaGraphNode_t knode = nullptr;
+    } si_graphs[2];
     // test hook (rtg_debug_si_wait_limit): applied to the next batched SI launch, then reset
     uint32_t dbg_wait_polls = 0, dbg_extra_tx = 0;
     int sm_count = 0;

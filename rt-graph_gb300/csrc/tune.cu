@@ -232,7 +232,7 @@ extern "C" rtg_status rtg_tune_si(rtg_ctx *ctx, const rtg_sets *s, const uint32_
     // the TC fields of the context's schedule are kept as they are
     rtg_config def = saved;
     def.si_block_warps = def.si_search_ratio = def.si_stage_slots = def.si_stage_bytes = 0;
-    def.si_blocks_per_sm = def.si_skew_stream = 0;
+    def.si_blocks_per_sm = def.si_skew_stream = def.si_form = 0;
     double def_ms = 0;
     rtg_status st = run(def, dwant, &def_ms);
     if (st != RTG_OK) {
@@ -242,32 +242,45 @@ extern "C" rtg_status rtg_tune_si(rtg_ctx *ctx, const rtg_sets *s, const uint32_
     RTG_CUDA(ctx, cudaMemcpy(hw.data(), dwant, npairs * 4, cudaMemcpyDeviceToHost));
     rtg_config best = def;
     double best_ms = def_ms;
+    auto consider = [&](const rtg_config &c, size_t smem) {
+        double ms = 0;
+        res->candidates++;
+        if (smem > (size_t)ctx->smem_optin || run(c, dgot, &ms) != RTG_OK ||
+            cudaMemcpy(hg.data(), dgot, npairs * 4, cudaMemcpyDeviceToHost) != cudaSuccess ||
+            hg != hw) {
+            res->rejected++;
+            return;
+        }
+        if (ms < best_ms) {
+            best_ms = ms;
+            best = c;
+        }
+    };
+    // per-warp rings: slot size x slots per warp x warps per block x search ratio
     for (uint32_t B : {2048u, 4096u, 8192u})
         for (uint32_t S : {2u, 3u, 4u})
             for (uint32_t W : {4u, 8u, 16u})
                 for (uint32_t ratio : {4u, 8u, 16u, 32u}) {
                     rtg_config c = def;
+                    c.si_form = 1;
                     c.si_stage_bytes = B;
                     c.si_stage_slots = S;
                     c.si_block_warps = W;
                     c.si_search_ratio = ratio;
-                    double ms = 0;
-                    res->candidates++;
-                    if ((size_t)W * S * (B + 512) + 4096 > (size_t)ctx->smem_optin ||
-                        run(c, dgot, &ms) != RTG_OK) {
-                        res->rejected++;
-                        continue;
-                    }
-                    if (cudaMemcpy(hg.data(), dgot, npairs * 4, cudaMemcpyDeviceToHost) !=
-                            cudaSuccess ||
-                        hg != hw) {
-                        res->rejected++;
-                        continue;
-                    }
-                    if (ms < best_ms) {
-                        best_ms = ms;
-                        best = c;
-                    }
+                    consider(c, (size_t)W * S * (B + 512) + 4096);
+                }
+    // producer/consumer: slot size x ring slots x merging warps per producer x search ratio
+    for (uint32_t B : {6144u, 8192u, 10240u})
+        for (uint32_t S : {3u, 4u, 5u, 6u})
+            for (uint32_t W : {2u, 3u, 4u})
+                for (uint32_t ratio : {8u, 16u}) {
+                    rtg_config c = def;
+                    c.si_form = 2;
+                    c.si_stage_bytes = B;
+                    c.si_stage_slots = S;
+                    c.si_block_warps = W;
+                    c.si_search_ratio = ratio;
+                    consider(c, (size_t)S * (B + 512) + 4096);
                 }
     {
         // the best schedule with skewed pairs staged and streamed instead of searched

@@ -53,7 +53,7 @@ class Config(C.Structure):
     _fields_ = [(k, C.c_uint32) for k in (
         "tc_block_warps", "tc_item_edges", "tc_region_words", "tc_blocks_per_sm",
         "si_block_warps", "si_search_ratio", "si_stage_slots", "si_stage_bytes",
-        "si_blocks_per_sm", "si_skew_stream")]
+        "si_blocks_per_sm", "si_skew_stream", "si_form")]
 
     def as_dict(self) -> dict:
         return {k: getattr(self, k) for k, _ in self._fields_}

@@ -32,7 +32,7 @@ def test_every_declared_symbol_is_exported():
 
 
 def test_status_strings_and_version():
-    assert rtg.lib.rtg_abi_version() == 2
+    assert rtg.lib.rtg_abi_version() == 3
     for s in range(10):
         assert rtg.lib.rtg_status_str(s)
     assert rtg.lib.rtg_status_str(99) == b"unknown status"

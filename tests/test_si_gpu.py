@@ -106,6 +106,17 @@ def test_generated_workload_known_answers(ctx, family):
     # skewed pairs staged and streamed (short list in the slot, long list in 16-byte loads)
     dict(si_skew_stream=1), dict(si_skew_stream=1, si_search_ratio=2),
     dict(si_skew_stream=1, si_stage_bytes=1024, si_stage_slots=3),
+    # the per-warp ring form named explicitly, then the producer/consumer form: its default,
+    # tiny slots (many chunk jobs whose counts meet in the block's accumulators), fewer ring
+    # slots than merging warps, long rings, one block per SM, every pair searched or merged,
+    # skewed pairs streamed
+    dict(si_form=1), dict(si_form=2), dict(si_form=2, si_stage_bytes=512),
+    dict(si_form=2, si_stage_bytes=512, si_stage_slots=2, si_block_warps=1),
+    dict(si_form=2, si_stage_slots=2, si_block_warps=8),
+    dict(si_form=2, si_stage_bytes=1024, si_stage_slots=32, si_block_warps=2),
+    dict(si_form=2, si_blocks_per_sm=1), dict(si_form=2, si_search_ratio=1),
+    dict(si_form=2, si_search_ratio=1000), dict(si_form=2, si_skew_stream=1),
+    dict(si_form=2, si_skew_stream=1, si_stage_bytes=1024, si_stage_slots=3),
 ])
 def test_batched_schedules_agree(ctx, cfg):
     """Small staging slots cut most pairs into many chunk pairs; results must not change."""
@@ -127,11 +138,13 @@ def test_batched_schedules_agree(ctx, cfg):
         ctx.set_config(**old.as_dict())
 
 
-def test_slot_and_ratio_boundaries(ctx):
-    """Default batched schedule (4 KB slots: 1024 words for both widened lists and their
-    sentinels; search ratio 8): pairs whose words land just under, on and just over one
-    slot, for every 16-byte alignment of either list's start, and pairs on either side of
-    |B| = 8 |A| both inside one slot and beyond it. Counts agree with the oracle."""
+@pytest.mark.parametrize("form,slot_bytes", [(1, 0), (2, 4096), (2, 0)])
+def test_slot_and_ratio_boundaries(ctx, form, slot_bytes):
+    """4 KB staging slots (the per-warp form's default; 1024 words for both widened lists
+    and their sentinels; search ratio 8) in both kernel forms, and the producer/consumer
+    form's own default: pairs whose words land just under, on and just over one slot, for
+    every 16-byte alignment of either list's start, and pairs on either side of |B| = 8 |A|
+    both inside one slot and beyond it. Counts agree with the oracle."""
     rng = np.random.default_rng(17)
     lists = []
     for pad in range(4):  # a list of `pad` elements shifts the next list's alignment
@@ -148,7 +161,12 @@ def test_slot_and_ratio_boundaries(ctx):
     k = len(lists)
     pa, pb = np.meshgrid(np.arange(k, dtype=np.uint32), np.arange(k, dtype=np.uint32))
     pa, pb = pa.ravel(), pb.ravel()
-    got, _ = ctx.sets(off, el).count(pa, pb, rtg.SI_AUTO)
+    saved = ctx.config().as_dict()
+    try:
+        ctx.set_config(**dict(saved, si_form=form, si_stage_bytes=slot_bytes))
+        got, _ = ctx.sets(off, el).count(pa, pb, rtg.SI_AUTO)
+    finally:
+        ctx.set_config(**saved)
     assert np.array_equal(got, oracle.si_pairs(off, el, pa, pb))
 
 
@@ -210,7 +228,8 @@ def test_vertex_pair_queries_on_graph(ctx):
     assert np.array_equal(got, oracle.si_pairs(off, adj, u, v))
 
 
-def test_bounded_wait_runs_out_cleanly(ctx):
+@pytest.mark.parametrize("form", [1, 2])
+def test_bounded_wait_runs_out_cleanly(ctx, form):
     """A staging-slot wait that cannot complete (the test hook makes one slot expect 16
     bytes more than its copies bring; every copy still lands, nothing stays in flight)
     gives up after a short bound: the call returns RTG_ERR_TIMEOUT, nothing faults or
@@ -218,15 +237,20 @@ def test_bounded_wait_runs_out_cleanly(ctx):
     off, el, pa, pb, exp = rtg.gen_si_pairs(20_000, seed=9)
     sets = ctx.sets(off, el)
     out = np.empty(len(pa), np.uint32)
-    assert rtg.lib.rtg_debug_si_wait_limit(ctx.h, 256, 15) == rtg.ERR_INVALID_ARG
-    assert rtg.lib.rtg_debug_si_wait_limit(ctx.h, 256, 16) == rtg.OK
-    st = rtg.lib.rtg_si_count(ctx.h, sets.h, rtg._ptr(pa), rtg._ptr(pb), len(pa),
-                              rtg._ptr(out), rtg.SI_AUTO, None)
-    assert st == rtg.ERR_TIMEOUT
-    assert b"bounded device wait" in rtg.lib.rtg_last_error(ctx.h)
-    for _ in range(2):  # the hook applied to one launch only; the context stays usable
-        got, _ = sets.count(pa, pb, rtg.SI_AUTO)
-        assert np.array_equal(got, exp)
+    saved = ctx.config().as_dict()
+    try:
+        ctx.set_config(**dict(saved, si_form=form))
+        assert rtg.lib.rtg_debug_si_wait_limit(ctx.h, 256, 15) == rtg.ERR_INVALID_ARG
+        assert rtg.lib.rtg_debug_si_wait_limit(ctx.h, 256, 16) == rtg.OK
+        st = rtg.lib.rtg_si_count(ctx.h, sets.h, rtg._ptr(pa), rtg._ptr(pb), len(pa),
+                                  rtg._ptr(out), rtg.SI_AUTO, None)
+        assert st == rtg.ERR_TIMEOUT
+        assert b"bounded device wait" in rtg.lib.rtg_last_error(ctx.h)
+        for _ in range(2):  # the hook applied to one launch only; the context stays usable
+            got, _ = sets.count(pa, pb, rtg.SI_AUTO)
+            assert np.array_equal(got, exp)
+    finally:
+        ctx.set_config(**saved)
     sets.close()
 
 
@@ -257,12 +281,13 @@ def test_skewed_pairs_streamed_match_oracle(ctx):
     want = oracle.si_pairs(off, el, pa, pb)
     saved = ctx.config().as_dict()
     try:
-        for stream in (0, 1):
-            ctx.set_config(**dict(saved, si_skew_stream=stream))
-            got, _ = sets.count(pa, pb, rtg.SI_AUTO)
-            assert np.array_equal(got, want), stream
-            got, _ = sets.count(pb, pa, rtg.SI_AUTO)
-            assert np.array_equal(got, want), stream
+        for form in (1, 2):
+            for stream in (0, 1):
+                ctx.set_config(**dict(saved, si_skew_stream=stream, si_form=form))
+                got, _ = sets.count(pa, pb, rtg.SI_AUTO)
+                assert np.array_equal(got, want), (form, stream)
+                got, _ = sets.count(pb, pa, rtg.SI_AUTO)
+                assert np.array_equal(got, want), (form, stream)
     finally:
         ctx.set_config(**saved)
     sets.close()
