@@ -87,12 +87,6 @@ typedef enum rtg_orient {
     RTG_ORIENT_SYMMETRIC = 2
 } rtg_orient;
 
-/* Triangle-count execution forms.
- *  PLAIN   : one kernel launch per work bucket, one warp per oriented edge, host-driven,
- *            fixed default schedule.
- *  BATCHED : persistent kernel over a device work queue of (vertex, edge-range) items,
- *            out-list of the source vertex staged in shared memory, launched as one
- *            CUDA graph, schedule from the context configuration (autotuned). */
 /* Triangle-count forms. PLAIN: the reference's per-edge formulation (one warp per oriented
  * edge, one launch per degree/ratio bucket). BATCHED: the counting form streamed by the
  * persistent kernel from a device queue, replayed from a CUDA graph, autotunable.
@@ -189,6 +183,18 @@ const char *rtg_status_str(rtg_status s);
 int rtg_abi_version(void);
 rtg_status rtg_set_config(rtg_ctx *ctx, const rtg_config *cfg);
 rtg_status rtg_get_config(const rtg_ctx *ctx, rtg_config *cfg);
+/* 1 in the checked build (librtg_checked.so, compiled with RTG_CHECKED), 0 otherwise; no
+ * counterpart in the reference, which has no checked build. The checked build validates
+ * every CSR and counting form on the device before a count reads it (offsets, ids, row
+ * order, suffix ranges) and checks the indexes the counting kernels derive from them; a
+ * violation is reported as RTG_ERR_FORMAT through the device status word, never as a
+ * fault. */
+int rtg_checked_build(void);
+/* Test hook of the checked build (RTG_ERR_STATE in any other build); no counterpart in the
+ * reference. With on != 0, rtg_graph_load(RTG_FMT_RTG_CSR) checks a cache file's sizes and
+ * checksum only, not its structure, so that a forged form reaches the device-side checks.
+ * Process-wide. */
+rtg_status rtg_debug_skip_file_checks(int on);
 /* Cumulative number of librtg kernel launches on this context. */
 uint64_t rtg_kernel_launches(const rtg_ctx *ctx);
 rtg_status rtg_synchronize(rtg_ctx *ctx);
@@ -244,7 +250,8 @@ rtg_status rtg_graph_file_check(const char *path);
 void rtg_graph_destroy(rtg_graph *g);
 
 /* ------------------------------------------------------ triangle counting */
-/* Exact uint64 triangle count of the oriented CSR of g. */
+/* Exact uint64 triangle count of the oriented CSR of g (BATCHED and BUCKETED read its
+ * counting form, which is all a graph read from a counting-form-only cache file holds). */
 rtg_status rtg_tc_count(rtg_ctx *ctx, rtg_graph *g, rtg_tc_mode mode, uint64_t *out_total,
                         rtg_timing *timing);
 /* End to end from host edges: copy in, build the CSR with `orient`, count, copy the
@@ -336,9 +343,10 @@ rtg_status rtg_si_count(rtg_ctx *ctx, const rtg_sets *s, const uint32_t *pair_a,
  * (RTG_SI_AUTO) launch on ctx only: one warp of the staging kernel arms its shared-memory
  * barrier for extra_tx_bytes (a multiple of 16, not 0) that no copy brings, so that phase
  * never completes and its wait, bounded at max_polls polls (the kernel's waits default to
- * 2^22), runs out. The warp records RTG_ERR_TIMEOUT in the status word and leaves before
- * taking any pairs (the other warps count them all, with nothing in flight), and the call
- * returns RTG_ERR_TIMEOUT with the context still usable. */
+ * 2^22), runs out. The warp records RTG_ERR_TIMEOUT in the status word (in the per-warp
+ * form it then leaves before taking any pairs; in the producer/consumer form the producer
+ * arms a barrier of its own and goes on), nothing stays in flight, and the call returns
+ * RTG_ERR_TIMEOUT with the context still usable. */
 rtg_status rtg_debug_si_wait_limit(rtg_ctx *ctx, uint32_t max_polls, uint32_t extra_tx_bytes);
 /* Dense |A| x |B| in the reference's row-major order (bs.cu:93-96,148):
  * out[(a - a_begin) * (b_end - b_begin) + (b - b_begin)]. */

@@ -73,34 +73,49 @@ def _headers() -> list[Path]:
                   + list(HOST.glob("*.h")) + list(CLI.glob("*.h")))
 
 
-def _compile(src: Path, obj: Path) -> Path:
+def _compile(src: Path, obj: Path, extra: tuple[str, ...] = ()) -> Path:
     obj.parent.mkdir(parents=True, exist_ok=True)
     if src.suffix == ".cu":
-        cmd = [NVCC, *NVCC_FLAGS, "-c", str(src), "-o", str(obj)]
+        cmd = [NVCC, *NVCC_FLAGS, *extra, "-c", str(src), "-o", str(obj)]
     else:
-        cmd = [CXX, *CXX_FLAGS, f"-I{HOST}", "-c", str(src), "-o", str(obj)]
+        cmd = [CXX, *CXX_FLAGS, *extra, f"-I{HOST}", "-c", str(src), "-o", str(obj)]
     _run(cmd)
     return obj
 
 
-def build_lib(jobs: int | None = None) -> Path:
+# the library variants: the product, and the checked build (every CSR and counting form
+# validated on the device before a count, kernel indexes checked; see include/rtg.h)
+LIB_VARIANTS = {
+    "librtg.so": ("obj", ()),
+    "librtg_checked.so": ("obj_checked", ("-DRTG_CHECKED",)),
+}
+
+
+def build_lib(jobs: int | None = None, variants: tuple[str, ...] = tuple(LIB_VARIANTS)) -> Path:
     srcs = sorted(CSRC.glob("*.cu")) + sorted(CSRC.glob("*.cpp"))
     hdrs = _headers()
     todo = []
-    objs = []
-    for s in srcs:
-        o = BUILD / "obj" / (s.name + ".o")
-        objs.append(o)
-        if _stale(o, [s, *hdrs]):
-            todo.append((s, o))
+    links = []
+    for name in variants:
+        objdir, extra = LIB_VARIANTS[name]
+        objs = []
+        stale = False
+        for s in srcs:
+            o = BUILD / objdir / (s.name + ".o")
+            objs.append(o)
+            if _stale(o, [s, *hdrs]):
+                todo.append((s, o, extra))
+                stale = True
+        links.append((LIBDIR / name, objs, stale))
     with cf.ThreadPoolExecutor(max_workers=jobs or min(16, os.cpu_count() or 4)) as ex:
-        list(ex.map(lambda so: _compile(*so), todo))
+        list(ex.map(lambda t: _compile(*t), todo))
     LIBDIR.mkdir(parents=True, exist_ok=True)
-    if todo or _stale(LIB, objs):
-        tmp = LIB.with_suffix(".so.tmp")
-        _run([NVCC, *ARCH, "-shared", "-o", str(tmp), *map(str, objs),
-              "-Xcompiler", "-fopenmp", "-lgomp", "-lcudart"])
-        os.replace(tmp, LIB)
+    for lib, objs, stale in links:
+        if stale or _stale(lib, objs):
+            tmp = lib.with_suffix(".so.tmp")
+            _run([NVCC, *ARCH, "-shared", "-o", str(tmp), *map(str, objs),
+                  "-Xcompiler", "-fopenmp", "-lgomp", "-lcudart"])
+            os.replace(tmp, lib)
     return LIB
 
 

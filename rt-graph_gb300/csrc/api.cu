@@ -73,6 +73,8 @@ rtg_status check_status_word(rtg_ctx *ctx) {
     RTG_CUDA(ctx, cudaMemsetAsync(ctx->d_status, 0, sizeof(uint32_t), ctx->stream));
     if (st == kStatusTimeout)
         return fail(ctx, RTG_ERR_TIMEOUT, "a bounded device wait ran out (status word %u)", st);
+    if (st == kStatusBadForm)
+        return fail(ctx, RTG_ERR_FORMAT, "device-side CSR check failed (status word %u)", st);
     return fail(ctx, RTG_ERR_INVALID_ARG, "device-side input check failed (status word %u)", st);
 }
 
@@ -553,7 +555,10 @@ rtg_status rtg_tc_count(rtg_ctx *ctx, rtg_graph *g, rtg_tc_mode mode, uint64_t *
     if (!ctx || !g || !out_total) return RTG_ERR_INVALID_ARG;
     if (mode != RTG_TC_PLAIN && mode != RTG_TC_BATCHED && mode != RTG_TC_BUCKETED)
         return fail(ctx, RTG_ERR_INVALID_ARG, "unknown tc mode %d", (int)mode);
-    if (!g->ori.built) return fail(ctx, RTG_ERR_STATE, "oriented CSR not built");
+    // PLAIN reads the oriented CSR; the other forms the counting form, which a graph read
+    // from a cache file may hold alone
+    if (mode == RTG_TC_PLAIN ? !g->ori.built : !(g->ori.built || g->cnt.built))
+        return fail(ctx, RTG_ERR_STATE, "oriented CSR not built");
     rtg_timing t{};
     double t0 = now_ms();
     RTG_TRY(tc_count(ctx, g, mode, out_total, &t));
@@ -1083,6 +1088,7 @@ rtg_status rtg_tc_list(rtg_ctx *ctx, rtg_graph *g, uint64_t *out_offsets, uint32
     if (!c.built) return fail(ctx, RTG_ERR_STATE, "oriented CSR not built (rtg_csr_build)");
     if (c.m > 0xFFFFFFFFull)
         return fail(ctx, RTG_ERR_INVALID_ARG, "at most 2^32-1 oriented edges for listing");
+    if (kChecked) RTG_TRY(check_csr(ctx, c, false));
     double t0 = now_ms();
     uint64_t l0 = ctx->launches;
     // the pairs are the edges themselves: (row of e, adj[e]) over the CSR's own rows
@@ -1115,6 +1121,7 @@ rtg_status rtg_graph_pair_count(rtg_ctx *ctx, rtg_graph *g, const uint32_t *u, c
     if (!g->sym.built) return fail(ctx, RTG_ERR_STATE, "symmetric CSR not built");
     if (npairs > 0xFFFFFFFFull)
         return fail(ctx, RTG_ERR_INVALID_ARG, "at most 2^32-1 pairs per call");
+    if (kChecked) RTG_TRY(check_csr(ctx, g->sym, false));
     PairSpec ps;
     ps.off = g->sym.off;
     ps.elems = g->sym.adj;

@@ -21,6 +21,17 @@ constexpr uint32_t kEmpty = 0xFFFFFFFFu;
 constexpr uint32_t kStatusOk = 0;
 constexpr uint32_t kStatusTimeout = 1;
 constexpr uint32_t kStatusBadInput = 2;
+constexpr uint32_t kStatusBadForm = 3;  // a CSR or counting form failed a device-side check
+
+// The checked build (compiled with -DRTG_CHECKED into librtg_checked.so): every CSR and
+// counting form is validated on the device before a count reads it, and the hot kernels
+// check the indexes they derive from it; a violation writes the status word (the call
+// returns RTG_ERR_FORMAT or RTG_ERR_INVALID_ARG) instead of reaching memory it must not.
+#ifdef RTG_CHECKED
+constexpr bool kChecked = true;
+#else
+constexpr bool kChecked = false;
+#endif
 
 struct DeviceBuffer {
     void *ptr = nullptr;
@@ -174,6 +185,17 @@ rtg_status build_count_direct(rtg_ctx *ctx, rtg_graph *g, bool in_scratch = fals
                               bool raw_degree = false, const EdgePrePass *pre = nullptr);
 rtg_status graph_free_csr(Csr &c);
 void count_csr_free(CountCsr &cc);
+
+// Device-side validation (check.cu): offsets non-decreasing from 0 to m, ids below n, rows
+// strictly ascending (and, for an oriented CSR, above their vertex); for a counting form
+// also its in-edge offsets and every suffix range inside one row, above its head. A
+// violation returns RTG_ERR_FORMAT. Every read index is a loop counter or a value checked
+// against its array's size first, so a forged form is refused without a fault.
+rtg_status check_csr(rtg_ctx *ctx, const Csr &c, bool above_vertex);
+rtg_status check_count_form(rtg_ctx *ctx, const CountCsr &cc);
+// test hook of the checked build: rtg_graph_load(RTG_FMT_RTG_CSR) skips the host-side
+// structure checks of a cache file (sizes and checksum are still checked)
+extern bool g_skip_file_structure_checks;
 
 // Triangle counting (tc.cu)
 rtg_status tc_count(rtg_ctx *ctx, rtg_graph *g, rtg_tc_mode mode, uint64_t *total,

@@ -609,13 +609,19 @@ __device__ __forceinline__ uint32_t consume_skew(const uint32_t *mt, uint32_t *s
 // its landed copies): per-segment counts accumulate into cnt[segment] (per-warp shared
 // counters). Jobs of other kinds have no segments and pass through.
 __device__ __forceinline__ void consume_slot(uint32_t *mt, uint32_t *slot, uint32_t *cnt,
-                                             uint32_t ratio, int lane) {
+                                             uint32_t ratio, uint32_t slot_words,
+                                             uint32_t *status, int lane) {
     const uint32_t nseg = mt[0];
     // per segment: a sentinel after each list (its reserved word; copies have landed) and
     // its merged or searched length, scanned into the segments' first diagonal / element
     uint32_t m = 0, sv = 0;
     if ((uint32_t)lane < nseg) {
-        const uint32_t la = mt[kLenA + lane], lb = mt[kLenB + lane];
+        uint32_t la = mt[kLenA + lane], lb = mt[kLenB + lane];
+        if (kChecked && (mt[kOffA + lane] + la >= slot_words || mt[kOffB + lane] + lb >= slot_words)) {
+            atomicExch(status, kStatusBadInput);  // a segment past its slot: dropped
+            la = lb = 0;
+            mt[kLenA + lane] = mt[kLenB + lane] = 0;
+        }
         if (la) {
             slot[mt[kOffA + lane] + la] = kEmpty;
             slot[mt[kOffB + lane] + lb] = kEmpty;
@@ -771,7 +777,7 @@ __global__ void __maxnreg__(80) k_si_stream(SiArgs s, uint32_t *out, unsigned lo
         uint32_t *mt = meta + sr * kMetaWords;
         uint32_t *slot = ring + (size_t)sr * p.slot_words;
         const uint32_t nseg = mt[0], kind = mt[1];
-        consume_slot(mt, slot, cnt, p.ratio, lane);
+        consume_slot(mt, slot, cnt, p.ratio, p.slot_words, status, lane);
         const uint64_t obase = (uint64_t)mt[2] | ((uint64_t)mt[3] << 32);
         if (kind == kJobSkew) {
             const uint32_t c = consume_skew(mt, slot, lane);
@@ -1079,7 +1085,7 @@ __global__ void __maxnreg__(96)
             continue;
         }
         const uint32_t nseg = mt[0];
-        consume_slot(mt, slot, cnt, p.ratio, lane);
+        consume_slot(mt, slot, cnt, p.ratio, p.slot_words, status, lane);
         if (kind == kJobSkew) {
             const uint32_t c = consume_skew(mt, slot, lane);
             if (lane == 0) out[obase] = c;

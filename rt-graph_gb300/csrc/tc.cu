@@ -210,6 +210,8 @@ struct WarpCfg {
     uint32_t n;      // vertices of the counting form
     uint32_t first;  // one-item-per-warp launches: the items [first, last) of `items`
     uint32_t last;
+    uint64_t m;        // edges of the counting form (checked build: range checks)
+    uint32_t *status;  // device status word (checked build: index violations)
 };
 
 // 1 << s for s < 32, 0 for s >= 32 (PTX clamps the shift amount; C++ leaves it undefined)
@@ -295,15 +297,22 @@ template <class F>
 __device__ __forceinline__ uint32_t stream_item(const uint32_t *__restrict__ adj,
                                                 const uint2 *__restrict__ rng, uint32_t k0,
                                                 uint32_t k1, int lane, uint32_t idle,
-                                                uint2 *cmp, uint2 first, F f) {
+                                                uint2 *cmp, uint2 first, F f,
+                                                const WarpCfg &p) {
     uint32_t cnt = 0;
     const uint32_t le = 0xFFFFFFFFu >> (31 - lane);  // lanes 0..lane
     const uint32_t lt = (1u << lane) - 1u;           // lanes below this one
     const uint32_t *adjl = adj + lane;
     uint2 nx = first;  // ranges of the first batch, loaded by the caller
     for (uint32_t kb = k0; kb < k1; kb += 32) {
-        const uint2 r = nx;
+        uint2 r = nx;
         nx = (kb + 32 + lane < k1) ? __ldg(rng + kb + 32 + lane) : make_uint2(0u, 0u);
+        if constexpr (kChecked) {
+            if (r.x > r.y || r.y > p.m) {  // a range outside the edges: refused, skipped
+                atomicExch(p.status, kStatusBadForm);
+                r = make_uint2(0u, 0u);
+            }
+        }
         const uint32_t len = r.y - r.x;  // 0 past the item
         // ---- 1. units
         cnt += stream_units<4>(adjl, len >> 7, r.x, lane, idle, f);
@@ -406,6 +415,13 @@ __global__ void __maxnreg__(48) k_tc_warp(const uint64_t *__restrict__ off, cons
         }
         const uint64_t it = items[k];
         const uint32_t v = (uint32_t)(it >> 32), k0 = (uint32_t)it;
+        if constexpr (kChecked) {
+            if (v >= p.n) {
+                if (lane == 0) atomicExch(p.status, kStatusBadForm);
+                if (!kPersistent) break;
+                continue;
+            }
+        }
         const uint64_t ov = off[v];
         const uint32_t b = (uint32_t)(off[v + 1] - ov);
         const uint64_t kin = in_off[v];
@@ -426,10 +442,21 @@ __global__ void __maxnreg__(48) k_tc_warp(const uint64_t *__restrict__ off, cons
                 const uint32_t w = __ldg(Nv + q);
                 if (w >= W0) {
                     const uint32_t o = w - W0;
+                    if (kChecked && (w >= p.n || (o >> 5) >= p.R)) {
+                        atomicExch(p.status, kStatusBadForm);
+                        continue;
+                    }
                     atomicOr(&reg[o >> 5], 1u << (o & 31));
                 } else {
                     uint32_t sl = hash_slot(w, kLowHashLg);
-                    while (atomicCAS(&tab[sl], 0u, w) != 0u) sl = (sl + 1) & (kLowHashWords - 1);
+                    uint32_t probes = 0;
+                    while (atomicCAS(&tab[sl], 0u, w) != 0u) {
+                        sl = (sl + 1) & (kLowHashWords - 1);
+                        if (kChecked && ++probes >= kLowHashWords) {  // table full
+                            atomicExch(p.status, kStatusBadForm);
+                            break;
+                        }
+                    }
                 }
             }
         }
@@ -438,22 +465,35 @@ __global__ void __maxnreg__(48) k_tc_warp(const uint64_t *__restrict__ off, cons
         // of 32); idle lanes read the guard word reg[R]
         const uint32_t *regp = reg - (W0 >> 5);
         const uint32_t idle = W0 + RB;
+        // checked build: an element outside [W0, W0 + 32 R] (the idle value W0 + 32 R reads
+        // the guard word) would read another warp's region
+        auto outside = [&](uint32_t w) -> bool {
+            if (w - W0 <= RB) return false;
+            atomicExch(p.status, kStatusBadForm);
+            return true;
+        };
         if (mode == 0) {
             cnt += stream_item(adj, in_rng + kin, k0, k1, lane, idle, cmp, first,
                                [&](uint32_t w) -> uint32_t {
+                                   if (kChecked && outside(w)) return 0u;
                                    return __funnelshift_r(regp[w >> 5], 0u, w) & 1u;
-                               });
+                               }, p);
         } else if (mode == 1) {
             cnt += stream_item(adj, in_rng + kin, k0, k1, lane, idle, cmp, first, [&](uint32_t w) -> uint32_t {
-                if (w >= W0) return __funnelshift_r(regp[w >> 5], 0u, w) & 1u;
+                if (w >= W0) {
+                    if (kChecked && outside(w)) return 0u;
+                    return __funnelshift_r(regp[w >> 5], 0u, w) & 1u;
+                }
                 uint32_t sl = hash_slot(w, kLowHashLg);
                 uint32_t x = tab[sl];
+                uint32_t probes = 0;
                 while (x != w && x != 0u) {
                     sl = (sl + 1) & (kLowHashWords - 1);
                     x = tab[sl];
+                    if (kChecked && ++probes >= kLowHashWords) break;
                 }
                 return x == w ? 1u : 0u;
-            });
+            }, p);
         } else {
             for (uint32_t kk = k0; kk < k1; ++kk) {
                 const uint2 r = __ldg(in_rng + kin + kk);
@@ -553,6 +593,8 @@ rtg_status batched_shape(rtg_ctx *ctx, const CountCsr &c, const rtg_config &cfg,
     bs->pc.E = cfg.tc_item_edges;
     bs->pc.R = cfg.tc_region_words;
     bs->pc.n = c.n;
+    bs->pc.m = c.m;
+    bs->pc.status = ctx->d_status;
     bs->smem = (size_t)bs->W * region_words(bs->pc.R) * 4;
     if (bs->smem + 256 > (size_t)ctx->smem_optin)
         return fail(ctx, RTG_ERR_INVALID_ARG, "schedule needs %zu B of shared memory", bs->smem);
@@ -884,6 +926,7 @@ rtg_status tc_launch_direct(rtg_ctx *ctx, rtg_graph *g, void *scratch, uint64_t 
     }
     if (tc_plan_estimate_bytes(ctx, g) > scratch_bytes)
         return fail(ctx, RTG_ERR_INVALID_ARG, "scratch too small for the count");
+    if (kChecked) RTG_TRY(check_count_form(ctx, c));
     BatchedShape bs{};
     RTG_TRY(batched_shape(ctx, c, effective_config(ctx, c.m), &bs));
     // scratch: acc (64 B) | items | vertex counts and offsets | scan temporary
@@ -911,6 +954,7 @@ rtg_status tc_launch_async(rtg_ctx *ctx, rtg_graph *g, unsigned long long *h_tot
         *h_total = 0;
         return RTG_OK;
     }
+    if (kChecked) RTG_TRY(check_count_form(ctx, c));
     TcPlan *p = nullptr;
     RTG_TRY(batched_plan(ctx, g, &p));
     RTG_CUDA(ctx, cudaGraphLaunch(p->exec, ctx->stream));
@@ -927,14 +971,24 @@ void tc_plan_release(rtg_graph *g) {
 rtg_status tc_count(rtg_ctx *ctx, rtg_graph *g, rtg_tc_mode mode, uint64_t *total,
                     rtg_timing *t) {
     const Csr &c = g->ori;
-    if (c.n > 0x7FFFFFFFu || c.m >= (1ull << 32))
+    const CountCsr &cc = g->cnt;
+    // a graph read from a cache file may hold its counting form alone
+    const bool form_only = !c.built && cc.built;
+    const uint32_t n = form_only ? cc.n : c.n;
+    const uint64_t m = form_only ? cc.m : c.m;
+    if (n > 0x7FFFFFFFu || m >= (1ull << 32))
         return fail(ctx, RTG_ERR_INVALID_ARG, "graph too large for 32-bit edge ids");
     t->algo_bytes = 4 * c.work_elems + 8 * c.m;
-    if (c.m == 0) {
+    if (m == 0) {
         *total = 0;
         return RTG_OK;
     }
-    if (mode == RTG_TC_PLAIN) return count_plain(ctx, g, total, t);
+    if (mode == RTG_TC_PLAIN) {
+        if (!c.built) return fail(ctx, RTG_ERR_STATE, "oriented CSR not built");
+        if (kChecked) RTG_TRY(check_csr(ctx, c, false));
+        return count_plain(ctx, g, total, t);
+    }
+    if (kChecked) RTG_TRY(check_count_form(ctx, cc));
     if (mode == RTG_TC_BUCKETED) return count_bucketed(ctx, g, total, t);
     return count_batched(ctx, g, total, t);
 }

@@ -144,6 +144,8 @@ _SIGS = {
     "rtg_graph_pair_count": (C.c_int, [P, P, P, P, C.c_uint64, P, C.c_uint32,
                                        C.POINTER(Timing)]),
     "rtg_debug_si_wait_limit": (C.c_int, [P, C.c_uint32, C.c_uint32]),
+    "rtg_checked_build": (C.c_int, []),
+    "rtg_debug_skip_file_checks": (C.c_int, [C.c_int]),
     "rtg_tc_count_device_csr_noalloc": (C.c_int, [P, P, C.c_uint32, C.c_uint64, u64p, P]),
     "rtg_sets_from_host": (C.c_int, [P, P, C.c_uint64, P, C.POINTER(P)]),
     "rtg_sets_from_host_u32": (C.c_int, [P, P, C.c_uint32, P, C.POINTER(P)]),

@@ -144,3 +144,17 @@ def test_dataset_roundtrip(tmp_path):
     i2, o2, e2 = rtg.dataset_read(str(tmp_path / "x.s_data"))
     assert (i2.num_a, i2.num_b, i2.max_element, i2.intersection, i2.elems) == (2, 1, 100, 1, 5)
     assert np.array_equal(o2, off) and np.array_equal(e2, el)
+
+
+def test_checked_build_variant_loads_and_flags_itself():
+    """The checked library is a separate build: it reports itself and accepts the
+    file-check test hook, which the product library refuses (no GPU call)."""
+    import ctypes as C
+    from pathlib import Path
+    assert rtg.lib.rtg_checked_build() == 0
+    assert rtg.lib.rtg_debug_skip_file_checks(1) == rtg.ERR_STATE
+    checked = C.CDLL(str(Path(rtg.LIB_PATH).parent / "librtg_checked.so"))
+    checked.rtg_debug_skip_file_checks.argtypes = [C.c_int]
+    assert checked.rtg_checked_build() == 1
+    assert checked.rtg_debug_skip_file_checks(1) == rtg.OK
+    assert checked.rtg_debug_skip_file_checks(0) == rtg.OK
