@@ -301,20 +301,23 @@ enum : uint32_t { kPairZero = 0, kPairPacked = 1, kPairChunked = 2, kPairSkewed 
 __device__ __forceinline__ uint32_t merge_range_count(const uint32_t *A, uint32_t na,
                                                       const uint32_t *B, uint32_t nb,
                                                       uint32_t x0, uint32_t x1) {
+    // 32-bit shared-memory byte addresses throughout (2 % faster than generic pointers)
+    const uint32_t sA = smem_u32(A), sB = smem_u32(B);
     uint32_t lo = x0 > nb ? x0 - nb : 0u, hi = min(x0, na);
     while (lo < hi) {
         const uint32_t mid = (lo + hi) >> 1;
-        if (A[mid] <= B[x0 - 1 - mid]) lo = mid + 1;
+        if (lds_u32(sA + 4 * mid) <= lds_u32(sB + 4 * (x0 - 1 - mid))) lo = mid + 1;
         else hi = mid;
     }
-    const uint32_t *pa = A + lo, *pb = B + (x0 - lo);
-    uint32_t ai = *pa, bj = *pb, c = 0;
-    for (uint32_t d = x0; d < x1; ++d) {
+    uint32_t ia = sA + 4 * lo, ib = sB + 4 * (x0 - lo);
+    uint32_t ai = lds_u32(ia), bj = lds_u32(ib), c = 0;
+    for (uint32_t n = x1 - x0; n; --n) {
         const bool ta = ai <= bj;
         c += (ai == bj) ? 1u : 0u;
-        pa += ta ? 1 : 0;
-        pb += ta ? 0 : 1;
-        const uint32_t v = *(ta ? pa : pb);
+        const uint32_t inc = ta ? 4u : 0u;
+        ia += inc;
+        ib += 4u - inc;
+        const uint32_t v = lds_u32(ta ? ia : ib);
         ai = ta ? v : ai;
         bj = ta ? bj : v;
     }
@@ -328,6 +331,7 @@ __device__ __forceinline__ uint32_t merge_range_count(const uint32_t *A, uint32_
 // kernel at 80 registers, three resident blocks per SM).
 constexpr int kSkewIlp = 2;
 
+template <int kIlp = kSkewIlp>
 __device__ __forceinline__ uint32_t skew_search_count(const uint32_t *__restrict__ A, uint32_t a,
                                                       const uint32_t *__restrict__ B, uint32_t b,
                                                       int lane) {
@@ -336,10 +340,10 @@ __device__ __forceinline__ uint32_t skew_search_count(const uint32_t *__restrict
     const uint32_t smp = first < b ? __ldg(B + min(first + step, b) - 1) : kEmpty;
     const uint32_t iters = 33 - __clz(step);  // lower_bound over step elements converges
     uint32_t c = 0;
-    for (uint32_t i0 = 0; i0 < a; i0 += 32 * kSkewIlp) {
-        uint32_t x[kSkewIlp], lo[kSkewIlp], hi[kSkewIlp];
+    for (uint32_t i0 = 0; i0 < a; i0 += 32 * kIlp) {
+        uint32_t x[kIlp], lo[kIlp], hi[kIlp];
 #pragma unroll
-        for (int k = 0; k < kSkewIlp; ++k) {
+        for (int k = 0; k < kIlp; ++k) {
             const uint32_t idx = i0 + 32 * k + lane;
             x[k] = idx < a ? __ldg(A + idx) : kEmpty;
             uint32_t pos = 0;  // number of bucket maxima below x (at most 31)
@@ -351,7 +355,7 @@ __device__ __forceinline__ uint32_t skew_search_count(const uint32_t *__restrict
         }
         for (uint32_t it = 0; it < iters; ++it) {
 #pragma unroll
-            for (int k = 0; k < kSkewIlp; ++k) {
+            for (int k = 0; k < kIlp; ++k) {
                 if (lo[k] < hi[k]) {
                     const uint32_t mid = (lo[k] + hi[k]) >> 1;
                     if (__ldg(B + mid) < x[k]) lo[k] = mid + 1;
@@ -360,7 +364,7 @@ __device__ __forceinline__ uint32_t skew_search_count(const uint32_t *__restrict
             }
         }
 #pragma unroll
-        for (int k = 0; k < kSkewIlp; ++k)
+        for (int k = 0; k < kIlp; ++k)
             c += (i0 + 32 * k + lane < a && lo[k] < b && __ldg(B + lo[k]) == x[k]) ? 1u : 0u;
     }
     return c;
@@ -838,6 +842,7 @@ struct PcCfg {
     uint32_t probe_tx;
 };
 constexpr uint32_t kPcEnt = 16;
+constexpr int kPcSkewIlp = 4;  // skewed searches per lane in lockstep (merging warps)
 enum : uint32_t { kJobSearch = 4, kJobEnd = 5 };
 // meta words of a search job: short and long list lengths and addresses (two words each)
 constexpr uint32_t kSrA = 6, kSrB = 7, kSrLA = 8, kSrLB = 10;
@@ -1079,7 +1084,7 @@ __global__ void __maxnreg__(96)
                 (uint64_t)mt[kSrLB] | ((uint64_t)mt[kSrLB + 1] << 32));
             __syncwarp();
             if (lane == 0) mbar_arrive(empty + sl);  // no data in the slot: free it now
-            uint32_t c = skew_search_count(LA, a, LB, b, lane);
+            uint32_t c = skew_search_count<kPcSkewIlp>(LA, a, LB, b, lane);
             c = __reduce_add_sync(kFull, c);
             if (lane == 0) out[obase] = c;
             continue;
