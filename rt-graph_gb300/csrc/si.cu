@@ -226,14 +226,14 @@ constexpr uint32_t kMetaWords = 112;
 // Number of elements of the sorted list B (nb >= 1, B[nb] = kEmpty) below x: branch-free
 // lower bound over shared memory.
 __device__ __forceinline__ uint32_t smem_lower_bound(const uint32_t *B, uint32_t nb, uint32_t x) {
-    const uint32_t *first = B;
-    uint32_t len = nb;
+    const uint32_t b0 = smem_u32(B);
+    uint32_t first = b0, len = nb;
     while (len > 1) {
         const uint32_t half = len >> 1;
-        first = (first[half - 1] < x) ? first + half : first;
+        first = (lds_u32(first + 4 * (half - 1)) < x) ? first + 4 * half : first;
         len -= half;
     }
-    return (uint32_t)(first - B) + ((*first < x) ? 1u : 0u);
+    return (first - b0) / 4 + ((lds_u32(first) < x) ? 1u : 0u);
 }
 enum : uint32_t { kJobPacked = 0, kJobChunk = 1, kJobChunkLast = 2, kJobSkew = 3 };
 // meta word of a chunk job holding its accumulator entry (producer/consumer form)
