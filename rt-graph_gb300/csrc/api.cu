@@ -334,6 +334,7 @@ rtg_status rtg_graph_from_host_pairs(rtg_ctx *ctx, const int32_t *pairs, uint64_
 }
 
 rtg_status rtg_csr_build(rtg_ctx *ctx, rtg_graph *g, rtg_orient orient) {
+    NvtxRange nvtx_("rtg_csr_build");
     if (!ctx || !g) return RTG_ERR_INVALID_ARG;
     if (orient != RTG_ORIENT_DEGREE && orient != RTG_ORIENT_DEGREE_RAW_REF &&
         orient != RTG_ORIENT_SYMMETRIC)
@@ -552,6 +553,7 @@ rtg_status rtg_graph_from_host_csr(rtg_ctx *ctx, const int32_t *offsets, const i
 
 rtg_status rtg_tc_count(rtg_ctx *ctx, rtg_graph *g, rtg_tc_mode mode, uint64_t *out_total,
                         rtg_timing *timing) {
+    NvtxRange nvtx_("rtg_tc_count");
     if (!ctx || !g || !out_total) return RTG_ERR_INVALID_ARG;
     if (mode != RTG_TC_PLAIN && mode != RTG_TC_BATCHED && mode != RTG_TC_BUCKETED)
         return fail(ctx, RTG_ERR_INVALID_ARG, "unknown tc mode %d", (int)mode);
@@ -634,6 +636,7 @@ __global__ void k_edge_pull(const uint4 *__restrict__ hs, const uint4 *__restric
 rtg_status rtg_tc_count_host_edges(rtg_ctx *ctx, const uint32_t *src, const uint32_t *dst,
                                    uint64_t m, rtg_orient orient, rtg_tc_mode mode,
                                    uint64_t *out_total, rtg_timing *timing) {
+    NvtxRange nvtx_("rtg_tc_count_host_edges");
     if (!ctx || !out_total || (m && (!src || !dst))) return RTG_ERR_INVALID_ARG;
     if (orient == RTG_ORIENT_SYMMETRIC)
         return fail(ctx, RTG_ERR_INVALID_ARG, "triangle counting needs an oriented CSR");
@@ -689,7 +692,11 @@ rtg_status rtg_tc_count_host_edges(rtg_ctx *ctx, const uint32_t *src, const uint
             RTG_CUDA(ctx, cudaMemcpyAsync(tg.d_dst, dst, m * 4, cudaMemcpyHostToDevice, ctx->stream));
         }
         RTG_CUDA(ctx, cudaEventRecord(ctx->ev[7], ctx->stream));
-        rtg_status s = build_count_direct(ctx, g, true, true, have_pre ? &pre : nullptr);
+        rtg_status s;
+        {
+            NvtxRange r("one-shot counting-form build");
+            s = build_count_direct(ctx, g, true, true, have_pre ? &pre : nullptr);
+        }
         void *scr = nullptr;
         const uint64_t need = s == RTG_OK ? tc_plan_estimate_bytes(ctx, g) : 0;
         if (s == RTG_OK) s = scratch(ctx, 6, need, &scr);
@@ -703,7 +710,10 @@ rtg_status rtg_tc_count_host_edges(rtg_ctx *ctx, const uint32_t *src, const uint
             cudaError_t e = cudaEventRecord(ctx->ev[0], ctx->stream);
             if (e != cudaSuccess) s = cuda_fail(ctx, e, "event", __FILE__, __LINE__);
         }
-        if (s == RTG_OK) s = tc_launch_direct(ctx, g, scr, need, &h);
+        if (s == RTG_OK) {
+            NvtxRange r("one-shot batched count");
+            s = tc_launch_direct(ctx, g, scr, need, &h);
+        }
         if (s == RTG_OK) {
             cudaError_t e = cudaEventRecord(ctx->ev[1], ctx->stream);
             if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
@@ -752,6 +762,7 @@ rtg_status rtg_tc_count_host_edges(rtg_ctx *ctx, const uint32_t *src, const uint
 rtg_status rtg_tc_count_host_csr(rtg_ctx *ctx, const int32_t *offsets, const int32_t *adjs,
                                  int32_t nodes, int64_t edges, rtg_tc_mode mode,
                                  uint64_t *out_total, rtg_timing *timing) {
+    NvtxRange nvtx_("rtg_tc_count_host_csr");
     if (!ctx || !out_total) return RTG_ERR_INVALID_ARG;
     rtg_timing t{};
     double t0 = now_ms();
@@ -810,6 +821,7 @@ static rtg_status sets_finish(rtg_ctx *ctx, rtg_sets *s) {
 
 rtg_status rtg_sets_from_host(rtg_ctx *ctx, const uint64_t *offsets, uint64_t nsets,
                               const uint32_t *elems, rtg_sets **out) {
+    NvtxRange nvtx_("rtg_sets_from_host");
     if (!ctx || !out || !offsets) return RTG_ERR_INVALID_ARG;
     *out = nullptr;
     uint64_t ne = offsets[nsets];
@@ -971,6 +983,7 @@ rtg_status rtg_debug_si_wait_limit(rtg_ctx *ctx, uint32_t max_polls, uint32_t ex
 rtg_status rtg_si_count(rtg_ctx *ctx, const rtg_sets *s, const uint32_t *pair_a,
                         const uint32_t *pair_b, uint64_t npairs, uint32_t *out_counts,
                         uint32_t flags, rtg_timing *timing) {
+    NvtxRange nvtx_("rtg_si_count");
     if (!ctx || !s || (npairs && (!pair_a || !pair_b || !out_counts))) return RTG_ERR_INVALID_ARG;
     if (npairs > 0xFFFFFFFFull)
         return fail(ctx, RTG_ERR_INVALID_ARG, "at most 2^32-1 pairs per call");
@@ -985,6 +998,7 @@ rtg_status rtg_si_count(rtg_ctx *ctx, const rtg_sets *s, const uint32_t *pair_a,
 rtg_status rtg_si_count_dense(rtg_ctx *ctx, const rtg_sets *s, uint32_t a_begin, uint32_t a_end,
                               uint32_t b_begin, uint32_t b_end, uint32_t *out_counts,
                               uint32_t flags, rtg_timing *timing) {
+    NvtxRange nvtx_("rtg_si_count_dense");
     if (!ctx || !s || a_end < a_begin || b_end < b_begin || a_end > s->nsets ||
         b_end > s->nsets)
         return RTG_ERR_INVALID_ARG;
@@ -1051,6 +1065,7 @@ static rtg_status materialize_to_host(rtg_ctx *ctx, const PairSpec &ps, uint64_t
 rtg_status rtg_si_materialize(rtg_ctx *ctx, const rtg_sets *s, const uint32_t *pair_a,
                               const uint32_t *pair_b, uint64_t npairs, uint64_t *out_offsets,
                               uint32_t *out_elems, uint64_t out_capacity, rtg_timing *timing) {
+    NvtxRange nvtx_("rtg_si_materialize");
     if (!ctx || !s || !out_offsets || (npairs && (!pair_a || !pair_b))) return RTG_ERR_INVALID_ARG;
     if (npairs > 0xFFFFFFFFull)
         return fail(ctx, RTG_ERR_INVALID_ARG, "at most 2^32-1 pairs per call");
@@ -1083,6 +1098,7 @@ __global__ void k_row_ids(const uint64_t *off, uint32_t n, uint32_t *src) {
 
 rtg_status rtg_tc_list(rtg_ctx *ctx, rtg_graph *g, uint64_t *out_offsets, uint32_t *out_elems,
                        uint64_t out_capacity, rtg_timing *timing) {
+    NvtxRange nvtx_("rtg_tc_list");
     if (!ctx || !g || !out_offsets || (out_capacity && !out_elems)) return RTG_ERR_INVALID_ARG;
     const Csr &c = g->ori;
     if (!c.built) return fail(ctx, RTG_ERR_STATE, "oriented CSR not built (rtg_csr_build)");
@@ -1117,6 +1133,7 @@ rtg_status rtg_tc_list(rtg_ctx *ctx, rtg_graph *g, uint64_t *out_offsets, uint32
 rtg_status rtg_graph_pair_count(rtg_ctx *ctx, rtg_graph *g, const uint32_t *u, const uint32_t *v,
                                 uint64_t npairs, uint32_t *out, uint32_t flags,
                                 rtg_timing *timing) {
+    NvtxRange nvtx_("rtg_graph_pair_count");
     if (!ctx || !g || (npairs && (!u || !v || !out))) return RTG_ERR_INVALID_ARG;
     if (!g->sym.built) return fail(ctx, RTG_ERR_STATE, "symmetric CSR not built");
     if (npairs > 0xFFFFFFFFull)

@@ -2,6 +2,7 @@
 #pragma once
 
 #include <cuda_runtime.h>
+#include <nvtx3/nvToolsExt.h>
 
 #include <cstdint>
 #include <cstdio>
@@ -247,5 +248,15 @@ rtg_status si_materialize_device(rtg_ctx *ctx, const PairSpec &ps, uint64_t *d_o
                                  uint64_t *launches);
 
 double now_ms();
+
+// NVTX range around a library stage: named ranges in Nsight Systems timelines and for
+// Nsight Compute's --nvtx filters, next to nothing when no tool is attached (NVTX v3 is
+// header-only).
+struct NvtxRange {
+    explicit NvtxRange(const char *name) { nvtxRangePushA(name); }
+    ~NvtxRange() { nvtxRangePop(); }
+    NvtxRange(const NvtxRange &) = delete;
+    NvtxRange &operator=(const NvtxRange &) = delete;
+};
 
 }  // namespace rtg

@@ -92,6 +92,7 @@ using namespace rtg;
 
 extern "C" rtg_status rtg_tune_tc(rtg_ctx *ctx, rtg_graph *g, const char *cache_path,
                                   rtg_tune_result *res) {
+    NvtxRange nvtx_("rtg_tune_tc");
     if (!ctx || !g || !res) return RTG_ERR_INVALID_ARG;
     memset(res, 0, sizeof *res);
     if (!g->ori.built || !g->cnt.built) return fail(ctx, RTG_ERR_STATE, "oriented CSR not built");
@@ -169,6 +170,7 @@ extern "C" rtg_status rtg_tune_tc(rtg_ctx *ctx, rtg_graph *g, const char *cache_
 extern "C" rtg_status rtg_tune_si(rtg_ctx *ctx, const rtg_sets *s, const uint32_t *pair_a,
                                   const uint32_t *pair_b, uint64_t npairs,
                                   const char *cache_path, rtg_tune_result *res) {
+    NvtxRange nvtx_("rtg_tune_si");
     if (!ctx || !s || !res || !npairs || !pair_a || !pair_b) return RTG_ERR_INVALID_ARG;
     memset(res, 0, sizeof *res);
     std::vector<uint64_t> off(s->nsets + 1);
