@@ -1,8 +1,9 @@
 """Child process of tests/test_checked_gpu.py: runs against the library named by RTG_LIB
 (the checked build) and exits non-zero on any mismatch.
 
-  parity  – triangle counts of golden graphs in every form and batched set intersections
-            in both kernel forms, against the golden counts and the oracle
+  parity  – triangle counts of golden graphs in every form, batched set intersections in
+            both kernel forms and one serving round (a count and a pair batch), against the
+            golden counts and the oracle
   forged  – counting forms forged to break one invariant each, loaded past the host-side
             file check (the checked build's test hook), are refused by the device-side
             check with RTG_ERR_FORMAT, and the context keeps counting correctly
@@ -49,6 +50,20 @@ def parity() -> None:
             assert np.array_equal(got, exp), form
         ctx.set_config(**saved)
         sets.close()
+    # the serving engine (its own contexts and launches) through the checked library
+    s, d = rtg.gen_rmat(11, 16, seed=7)
+    want = oracle.tc_merge(*oracle.degree_csr(s, d))
+    soff, sadj = oracle.symmetric_csr(s, d)
+    u = np.arange(0, 4000, dtype=np.uint32) % (len(soff) - 1)
+    v = (u * 7 + 3) % (len(soff) - 1)
+    with rtg.Server(0, held=True) as srv:
+        gid = srv.add_graph(s, d)
+        rt = srv.submit_tc(gid)
+        rp, out = srv.submit_pairs(gid, u, v)
+        srv.release()
+        assert srv.poll(rt)["triangles"] == want
+        assert srv.poll(rp)["status"] == rtg.OK
+        assert np.array_equal(out, oracle.si_pairs(soff, sadj, u, v))
 
 
 def forged() -> None:
