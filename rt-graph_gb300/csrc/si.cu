@@ -811,7 +811,7 @@ __global__ void __maxnreg__(80) k_si_stream(SiArgs s, uint32_t *out, unsigned lo
 // and issues their bulk copies into a ring of R slots shared by the block; W consumer warps
 // take the jobs in order by tickets (job t lives in slot t mod R) and only merge / search.
 // The producer runs up to R jobs ahead, so copies stay in flight while the consumers merge,
-// and job formation and the long skewed searches leave the consumers' path:
+// and job formation leaves the consumers' path:
 //   full[r]  – completes when slot r's job is posted and its copies have landed
 //              (one arrival by the producer + the copies' bytes);
 //   empty[r] – completes when the consumer of slot r's job is done with it (one arrival);
