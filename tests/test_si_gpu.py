@@ -291,3 +291,22 @@ def test_skewed_pairs_streamed_match_oracle(ctx):
     finally:
         ctx.set_config(**saved)
     sets.close()
+
+
+@pytest.mark.parametrize("cfg", [dict(), dict(si_form=2, si_stage_bytes=512, si_stage_slots=3),
+                                 dict(si_form=1, si_stage_bytes=1024)])
+def test_batched_counts_repeat_exactly(ctx, cfg):
+    """The batched forms hand out jobs dynamically (queue, tickets) and add chunk counts with
+    atomics, so which warp does what changes from run to run; the counts must not: ten runs
+    of the same pairs, every one equal to the generator's known answers."""
+    off, el, pa, pb, exp = rtg.gen_si_pairs(20_000, seed=13)
+    sets = ctx.sets(off, el)
+    saved = ctx.config().as_dict()
+    try:
+        ctx.set_config(**dict(saved, **cfg))
+        for _ in range(10):
+            got, _ = sets.count(pa, pb, rtg.SI_AUTO)
+            assert np.array_equal(got, exp)
+    finally:
+        ctx.set_config(**saved)
+    sets.close()
