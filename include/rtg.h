@@ -89,10 +89,13 @@ typedef enum rtg_orient {
 
 /* Triangle-count forms. PLAIN: the reference's per-edge formulation (one warp per oriented
  * edge, one launch per degree/ratio bucket). BATCHED: the counting form streamed by the
- * persistent kernel from a device queue, replayed from a CUDA graph, autotunable.
- * BUCKETED: the same counting-form kernel without persistence or graph: work items built
- * on every call, one launch per item-size bucket with one warp per item, the library's
- * default schedule (it separates what the algorithm and what the scheduling contribute). */
+ * persistent kernel from a device queue, replayed from a CUDA graph, autotunable; edges
+ * among the top ranks (the dense core, rtg_config.tc_core_ranks) are counted as word ANDs
+ * of the core's adjacency bit matrix, the other in-edges are streamed. BUCKETED: the same
+ * counting-form kernels without persistence or graph: work items built on every call, one
+ * launch per item-size bucket with one warp per item, the library's default schedule and
+ * the context's core setting (it separates what the algorithm and what the scheduling
+ * contribute). */
 typedef enum rtg_tc_mode { RTG_TC_PLAIN = 0, RTG_TC_BATCHED = 1, RTG_TC_BUCKETED = 2 } rtg_tc_mode;
 
 /* Set-intersection execution forms (flags of rtg_si_count*).
@@ -129,6 +132,10 @@ typedef struct rtg_timing {
     uint64_t algo_bytes;      /* algorithmic bytes of the counting stage          */
     uint64_t h2d_bytes;
     uint64_t d2h_bytes;
+    double core_ms;           /* BATCHED / BUCKETED count: the dense-core stage (core
+                                 matrix build + core count), part of count_ms        */
+    uint32_t core_ranks;      /* ... and the top ranks it covered (0: no core)      */
+    uint32_t reserved;
 } rtg_timing;
 
 typedef struct rtg_graph_info {
@@ -171,7 +178,17 @@ typedef struct rtg_config {
                                    issues their bulk copies into a ring of si_stage_slots
                                    slots shared by si_block_warps merging warps; 0 = library
                                    default                                            */
+    uint32_t tc_core_ranks;     /* dense core of the BATCHED / BUCKETED triangle count: the
+                                   top min(value, n) ranks (1..32768) have their
+                                   adjacency held as a bit matrix, and their edges are
+                                   counted by word AND + popcount; RTG_TC_CORE_NONE: no
+                                   core; 0 = library choice (the largest of 16384, 8192,
+                                   4096, 2048, 1024 top ranks whose edge density is at
+                                   least 3 %, none if no such core)                  */
 } rtg_config;
+
+#define RTG_TC_CORE_NONE 0xFFFFFFFFu
+#define RTG_TC_CORE_MAX_RANKS 32768u
 
 /* ---------------------------------------------------------------- context */
 rtg_status rtg_init(int device, rtg_ctx **out);

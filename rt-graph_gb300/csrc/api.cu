@@ -199,6 +199,9 @@ rtg_status rtg_set_config(rtg_ctx *ctx, const rtg_config *cfg) {
         return fail(ctx, RTG_ERR_INVALID_ARG, "si_skew_stream must be 0 or 1");
     if (cfg->si_form > 2)
         return fail(ctx, RTG_ERR_INVALID_ARG, "si_form must be 0, 1 or 2");
+    if (cfg->tc_core_ranks > RTG_TC_CORE_MAX_RANKS && cfg->tc_core_ranks != RTG_TC_CORE_NONE)
+        return fail(ctx, RTG_ERR_INVALID_ARG,
+                    "tc_core_ranks must be 0, RTG_TC_CORE_NONE or in [1, 32768]");
     ctx->cfg = *cfg;
     return RTG_OK;
 }

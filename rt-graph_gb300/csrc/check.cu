@@ -61,8 +61,10 @@ __global__ void k_check_rows(const uint64_t *__restrict__ off, const uint32_t *_
 }
 
 // in-edge ranges of a counting form: in-edge e of head v (in_off[v] <= e < in_off[v + 1])
-// holds [x, y) with x <= y <= m; a non-empty range lies inside one row u of the CSR and
-// starts at an element above v (rows ascend, so all of it is above v)
+// holds [x, y) with x <= y <= m, x not below the previous in-edge's x (in-edges ordered by
+// source: the dense-core split takes those from core rows to be the last ones of v); a
+// non-empty range lies inside one row u of the CSR and starts at an element above v (rows
+// ascend, so all of it is above v)
 __global__ void k_check_ranges(const uint64_t *__restrict__ off, const uint32_t *__restrict__ adj,
                                const uint64_t *__restrict__ in_off,
                                const uint2 *__restrict__ in_rng, uint32_t n, uint64_t m,
@@ -71,7 +73,8 @@ __global__ void k_check_ranges(const uint64_t *__restrict__ off, const uint32_t 
          e += (uint64_t)gridDim.x * blockDim.x) {
         const uint2 r = in_rng[e];
         const uint32_t v = row_of(in_off, n, e);
-        if (v >= n || in_off[v] > e || e >= in_off[v + 1] || r.x > r.y || r.y > m) {
+        if (v >= n || in_off[v] > e || e >= in_off[v + 1] || r.x > r.y || r.y > m ||
+            (e > in_off[v] && in_rng[e - 1].x > r.x)) {
             bad_form(status);
             continue;
         }

@@ -242,7 +242,9 @@ rtg_status read_cache_file(const char *path, CacheFile &cf, std::string &why,
         // the batched kernel indexes its per-warp bitmap by (element - window origin) and
         // takes every element of a suffix of an in-edge of v to be a rank above v: every
         // row of v must hold ascending ranks above v, and every suffix range of an in-edge
-        // of v must lie inside one row and hold only ranks above v
+        // of v must lie inside one row and hold only ranks above v; the in-edges of v are
+        // ordered by source (a range never starts before the previous in-edge's), which the
+        // dense-core split relies on (the in-edges from core rows are the last ones of v)
         for (uint64_t v = 0; structure && v < hc.n; ++v)
             for (uint64_t q = hc.off[v]; q < hc.off[v + 1]; ++q)
                 if (hc.adj[q] <= v || (q > hc.off[v] && hc.adj[q] <= hc.adj[q - 1]))
@@ -251,6 +253,7 @@ rtg_status read_cache_file(const char *path, CacheFile &cf, std::string &why,
             for (uint64_t e = hc.in_off[v]; e < hc.in_off[v + 1]; ++e) {
                 const uint2 rg = hc.rng[e];
                 if (rg.x > rg.y || rg.y > hc.m) return bad("suffix range");
+                if (e > hc.in_off[v] && rg.x < hc.rng[e - 1].x) return bad("in-edge order");
                 if (rg.x == rg.y) continue;
                 // the row u holding position x: last offset <= x
                 uint64_t lo = 0, hi = hc.n;

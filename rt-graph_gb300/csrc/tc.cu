@@ -23,10 +23,24 @@
 //           sequence in full 32-lane windows, testing every element with one shared-memory
 //           load.
 //           Streamed elements: sum over u of d+(u)(d+(u)-1)/2, about a quarter of the
-//           push-order work on power-law graphs. The items are built once per (graph,
-//           schedule); the count (counter resets + the persistent kernel) is one CUDA graph,
-//           captured once and replayed. uint64 totals: lane partials -> warp shuffle sum ->
-//           block sum -> one atomicAdd per block.
+//           push-order work on power-law graphs.
+//           Dense core: on power-law graphs most of those elements belong to in-edges whose
+//           source sits among the top ranks (R-MAT scale 21: sources in the top 16,384 ranks
+//           stream 51 % of them, in a core whose edge density is 4.9 %). A triangle whose
+//           lowest vertex u lies in the top K ranks [c0, n) has all three vertices there,
+//           so the core's share of the count is the sum over core edges u->v of
+//           popcount(M[u] & M[v]), M the core's adjacency bit matrix (row r: N+(c0 + r) as
+//           bits of ranks from c0). The count builds M (one warp per row), counts the core
+//           edges word by word (k_tc_core: one warp per core row, the row staged in shared
+//           memory, the word ranges of all its edges swept as one flat sequence), and
+//           streams only the in-edges whose source lies below c0: the in-edges of a head
+//           are ordered by source, so those are the first sdeg[v] of them. K is picked on
+//           the device from the offsets when the items are built (the largest of 16384 ..
+//           1024 top ranks with edge density >= 3 %, or none), or set by the schedule.
+//           The items are built once per (graph, schedule); the count (counter resets,
+//           core matrix, core count, the persistent kernel) is one CUDA graph, captured
+//           once and replayed. uint64 totals: lane partials -> warp shuffle sum -> block
+//           sum -> one atomicAdd per block.
 #include <cub/cub.cuh>
 
 #include <algorithm>
@@ -152,29 +166,110 @@ __global__ void __launch_bounds__(256) k_plain_edges(const uint64_t *__restrict_
 
 // ---------------------------------------------------------------- BATCHED form
 
-// items per vertex v: ceil(indeg(v) / E) when v has out-neighbours and in-neighbours
+// acc (kAccWords u64 per count): [0] total, [1] item queue head, [2] number of items,
+// [3..5] items per size bucket (BUCKETED), [6] core queue head, [8] core ranks K (0: no
+// core), [9] c0 = n - K, [10] words per core matrix row, [11] off[c0] (the first adj index
+// of a core row)
+constexpr int kAccWords = 16;
+constexpr int kAccCoreQ = 6, kAccCoreK = 8, kAccCoreC0 = 9, kAccCoreRw = 10, kAccCoreXc = 11;
+
+// Core sizes the library picks from, and the edge density (per cent of K (K - 1) / 2) the
+// core must reach. Measured on R-MAT scale 18/20/21 (edge factor 16): the largest core of at
+// least 3 % density removes 40-55 % of the element work (cost model: 7 instructions per
+// streamed element, 5 per word of AND); on Holme-Kim and Barabasi-Albert graphs of 2^20
+// vertices no core reaches 2 %, and a 16K core there would add work.
+constexpr uint32_t kCoreAutoMax = 16384, kCoreAutoMin = 1024, kCoreMinDensityPct = 3;
+
+// The core count sweeps the matrix in groups of kCoreGroupWords words (16 bytes, one load per
+// lane and position). Measured on R-MAT scale 21 with 16384 core ranks: 0.25-0.27 ms with
+// 16-byte groups, 0.30 ms with 32-byte and 0.50 ms with 64-byte groups (a word range averages
+// 17 groups of 4 words but most are short, and wider groups sweep more zero words), 0.50 ms
+// with 4-byte positions (the per-position segment search then runs for every word).
+constexpr uint32_t kCoreGroupWords = 4;
+constexpr uint32_t kCoreVec = kCoreGroupWords / 4;
+
+// words of a core matrix row for K ranks: a power of two of at least one group, so that a
+// group's place within its row is its matrix group index masked
+__host__ __device__ constexpr uint32_t core_row_words(uint32_t K) {
+    uint32_t w = kCoreGroupWords;
+    while (w * 32 < K) w <<= 1;
+    return K ? w : 0u;
+}
+
+// largest core the schedule can pick on a graph of n vertices (sizes the core buffers)
+uint32_t core_max_ranks(uint32_t forced, uint32_t n) {
+    if (forced == RTG_TC_CORE_NONE) return 0;
+    if (forced) return std::min(forced, n);
+    for (uint32_t c = kCoreAutoMax; c >= kCoreAutoMin; c >>= 1)
+        if (c <= n) return c;
+    return 0;
+}
+
+// The core of this count: `forced` ranks (RTG_TC_CORE_NONE: none), or with forced == 0 the
+// largest candidate whose m - off[n - K] core edges reach the density bar.
+__global__ void k_core_pick(const uint64_t *__restrict__ off, uint32_t n, uint64_t m,
+                            uint32_t forced, unsigned long long *acc) {
+    if (blockIdx.x || threadIdx.x) return;
+    uint32_t K = 0;
+    if (forced == RTG_TC_CORE_NONE) K = 0;
+    else if (forced) K = min(forced, n);
+    else
+        for (uint32_t c = kCoreAutoMax; c >= kCoreAutoMin; c >>= 1) {
+            if (c > n) continue;
+            const uint64_t ce = m - off[n - c];
+            if (100ull * ce >= (uint64_t)kCoreMinDensityPct * c * (c - 1) / 2) {
+                K = c;
+                break;
+            }
+        }
+    acc[kAccCoreK] = K;
+    acc[kAccCoreC0] = n - K;
+    acc[kAccCoreRw] = core_row_words(K);
+    acc[kAccCoreXc] = off[n - K];
+}
+
+// Per vertex v: sdeg[v] = the in-edges streamed by the persistent kernel, those whose
+// suffix range starts before the first core row (x < off[c0]); the in-edges of a head are
+// ordered by source, and x grows with the source, so they are a prefix (binary search for
+// heads in the core, all in-edges below it; an empty range at the end of a row may count as
+// core, which drops nothing). Items per vertex: ceil(sdeg(v) / E) when v has out-neighbours.
 __global__ void k_item_counts(const uint64_t *__restrict__ off,
-                              const uint64_t *__restrict__ in_off, uint32_t n, uint32_t E,
-                              uint32_t *cnt) {
+                              const uint64_t *__restrict__ in_off,
+                              const uint2 *__restrict__ in_rng, uint32_t n, uint32_t E,
+                              const unsigned long long *acc, uint32_t *cnt, uint32_t *sdeg) {
+    const uint32_t c0 = (uint32_t)acc[kAccCoreC0];
+    const uint64_t xc = acc[kAccCoreXc];
     for (uint64_t v = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; v <= n;
          v += (uint64_t)gridDim.x * blockDim.x) {
         uint32_t c = 0;
         if (v < n) {
-            uint32_t b = (uint32_t)(off[v + 1] - off[v]);
-            uint32_t indeg = (uint32_t)(in_off[v + 1] - in_off[v]);
-            c = (b >= 1 && indeg >= 1) ? (indeg + E - 1) / E : 0u;
+            const uint32_t b = (uint32_t)(off[v + 1] - off[v]);
+            const uint64_t k0 = in_off[v];
+            const uint32_t indeg = (uint32_t)(in_off[v + 1] - k0);
+            uint32_t sd = indeg;
+            if (v >= c0 && indeg) {
+                uint32_t lo = 0, hi = indeg;
+                while (lo < hi) {
+                    const uint32_t mid = lo + (hi - lo) / 2;
+                    if (in_rng[k0 + mid].x < xc) lo = mid + 1;
+                    else hi = mid;
+                }
+                sd = lo;
+            }
+            sdeg[v] = sd;
+            c = (b >= 1 && sd >= 1) ? (sd + E - 1) / E : 0u;
         }
         cnt[v] = c;
     }
 }
 
-__global__ void k_item_fill(const uint64_t *__restrict__ off, const uint64_t *__restrict__ in_off,
+__global__ void k_item_fill(const uint64_t *__restrict__ off, const uint32_t *__restrict__ sdeg,
                             uint32_t n, uint32_t E, const uint32_t *__restrict__ base,
                             uint64_t *items, unsigned long long *acc) {
     for (uint64_t v = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; v < n;
          v += (uint64_t)gridDim.x * blockDim.x) {
         uint32_t b = (uint32_t)(off[v + 1] - off[v]);
-        uint32_t indeg = (uint32_t)(in_off[v + 1] - in_off[v]);
+        uint32_t indeg = sdeg[v];
         if (b < 1 || indeg < 1) continue;
         // descending rank order: the many light items of low-rank vertices come last and
         // fill in behind the heavier ones (1.4 % shorter than ascending order on R-MAT-21)
@@ -191,14 +286,14 @@ constexpr int kItemBuckets = 3;
 
 __global__ void k_item_bucket(const uint64_t *__restrict__ items,
                               const unsigned long long *__restrict__ nitems,
-                              const uint64_t *__restrict__ in_off, uint32_t E, uint64_t cap,
+                              const uint32_t *__restrict__ sdeg, uint32_t E, uint64_t cap,
                               uint64_t *out, unsigned long long *cnt) {
     const unsigned long long ni = *nitems;
     for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < ni;
          i += (uint64_t)gridDim.x * blockDim.x) {
         const uint64_t it = items[i];
         const uint32_t v = (uint32_t)(it >> 32), k0 = (uint32_t)it;
-        const uint32_t ne = min(E, (uint32_t)(in_off[v + 1] - in_off[v]) - k0);
+        const uint32_t ne = min(E, sdeg[v] - k0);
         const int r = ne <= 32 ? 0 : (ne <= 256 ? 1 : 2);
         out[r * cap + atomicAdd(&cnt[r], 1ull)] = it;
     }
@@ -371,8 +466,6 @@ __host__ __device__ constexpr uint32_t region_words(uint32_t R) {
     return R + 2 + kLowHashWords + kCmpWords;
 }
 
-// acc[0] = total, acc[1] = item queue head, acc[2] = number of items
-//
 // Per item the warp marks N+(v) in its shared-memory region: a bitmap of R words over the
 // ranks [W0, n) (W0 a multiple of 32), with W0 = v + 1 rounded down when n - W0 fits the
 // bitmap (high-rank v: every element of N+(v) and of the suffixes is in the window), else
@@ -387,6 +480,7 @@ __host__ __device__ constexpr uint32_t region_words(uint32_t R) {
 template <bool kPersistent>
 __global__ void __maxnreg__(48) k_tc_warp(const uint64_t *__restrict__ off, const uint32_t *__restrict__ adj,
                           const uint64_t *__restrict__ in_off, const uint2 *__restrict__ in_rng,
+                          const uint32_t *__restrict__ sdeg,
                           const uint64_t *__restrict__ items, unsigned long long *acc,
                           WarpCfg p) {
     extern __shared__ __align__(16) uint32_t smem[];
@@ -425,7 +519,7 @@ __global__ void __maxnreg__(48) k_tc_warp(const uint64_t *__restrict__ off, cons
         const uint64_t ov = off[v];
         const uint32_t b = (uint32_t)(off[v + 1] - ov);
         const uint64_t kin = in_off[v];
-        const uint32_t k1 = min(k0 + p.E, (uint32_t)(in_off[v + 1] - kin));
+        const uint32_t k1 = min(k0 + p.E, sdeg[v]);  // streamed in-edges: the first sdeg[v]
         const uint32_t *Nv = adj + ov;
         // the first batch of suffix ranges, loaded before the out-list is marked
         const uint2 first = (k0 + lane < k1) ? __ldg(in_rng + kin + k0 + lane) : make_uint2(0u, 0u);
@@ -516,6 +610,195 @@ __global__ void __maxnreg__(48) k_tc_warp(const uint64_t *__restrict__ off, cons
     block_add_total(cnt, &acc[0], red);
 }
 
+// ------------------------------------------------------------------ dense core
+
+// Core matrix rows: one warp per core row r (vertex c0 + r) sets the bits of N+(c0 + r) in a
+// shared-memory row of rw words, then writes the whole row (zeros included, so M needs no
+// separate clearing) and its word span [first, last] (span (1, 0): empty row). Also resets
+// the core queue head for k_tc_core, which runs next on the stream. Dynamic shared memory:
+// rw_max words per warp.
+__global__ void __launch_bounds__(256) k_core_rows(const uint64_t *__restrict__ off,
+                                                   const uint32_t *__restrict__ adj,
+                                                   unsigned long long *acc, uint32_t *core_m,
+                                                   uint2 *span, uint32_t rw_max,
+                                                   uint32_t *status) {
+    extern __shared__ __align__(16) uint32_t smem[];
+    if (blockIdx.x == 0 && threadIdx.x == 0) acc[kAccCoreQ] = 0ull;
+    const uint32_t K = (uint32_t)acc[kAccCoreK], c0 = (uint32_t)acc[kAccCoreC0],
+                   rw = (uint32_t)acc[kAccCoreRw];
+    if (!K || rw > rw_max) return;  // rw <= rw_max: the plan sized the buffers for its largest K
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    uint32_t *S = smem + (size_t)warp * rw_max;
+    for (uint32_t q = lane; q < rw; q += 32) S[q] = 0u;
+    __syncwarp();
+    const uint32_t nw = gridDim.x * (blockDim.x >> 5);
+    for (uint32_t r = blockIdx.x * (blockDim.x >> 5) + warp; r < K; r += nw) {
+        const uint64_t ou = off[c0 + r];
+        const uint32_t d = (uint32_t)(off[c0 + r + 1] - ou);
+        for (uint32_t q = lane; q < d; q += 32) {
+            const uint32_t o = __ldg(adj + ou + q) - c0;  // an element of a core row: >= c0
+            if (kChecked && o >= K) {
+                atomicExch(status, kStatusBadForm);
+                continue;
+            }
+            atomicOr(&S[o >> 5], 1u << (o & 31));
+        }
+        __syncwarp();
+        uint32_t *row = core_m + (size_t)r * rw;
+        for (uint32_t q = lane; q < rw; q += 32) {
+            row[q] = S[q];
+            S[q] = 0u;
+        }
+        if (lane == 0)
+            span[r] = d ? make_uint2((__ldg(adj + ou) - c0) >> 5, (__ldg(adj + ou + d - 1) - c0) >> 5)
+                        : make_uint2(1u, 0u);
+        __syncwarp();
+    }
+}
+
+// Per-warp shared memory of k_tc_core: the staged row (rw_max words) and the compacted
+// segments of a batch of 32 edges (first group, matrix row, length: 3 x 32 words).
+__host__ __device__ constexpr uint32_t core_region_words(uint32_t rw_max) { return rw_max + 96; }
+constexpr int kCoreWin = 4;  // 32-position windows whose loads are in flight together
+
+// Core count: warps take core rows r from the queue (acc[kAccCoreQ]), heaviest (lowest rank)
+// first; for u = c0 + r the warp copies the groups of M[u] that hold its span into shared
+// memory, and for each batch of 32 edges u->v (lane k: edge k; the last edge of the row has
+// no later element and is skipped) takes the groups of N+(v)'s span up to u's last group (a
+// group reaches past a span only over zero words of M[v] or of the staged row, so whole
+// groups count exactly). The non-empty group ranges are compacted and swept as one flat
+// sequence in 32-position windows with every lane busy: the segment of position q is found
+// from the segment starts inside the window (one OR-reduction of a bit per segment) and
+// gives the matrix group by one shuffle; the group within the row (the staged row's group)
+// is that index masked. Group g of edge u->v adds the popcounts of M[u][g] & M[v][g],
+// kCoreGroupWords words, 16-byte loads from each. M[v] comes from L2 (the matrix, 32 MB
+// for 16384 ranks, is written by k_core_rows just before).
+__global__ void __launch_bounds__(256) k_tc_core(const uint64_t *__restrict__ off,
+                                                 const uint32_t *__restrict__ adj,
+                                                 const uint32_t *__restrict__ core_m,
+                                                 const uint2 *__restrict__ span,
+                                                 unsigned long long *acc, uint32_t rw_max,
+                                                 uint32_t *status) {
+    extern __shared__ __align__(16) uint32_t smem[];
+    __shared__ unsigned long long red[32];
+    const uint32_t K = (uint32_t)acc[kAccCoreK], c0 = (uint32_t)acc[kAccCoreC0],
+                   rw = (uint32_t)acc[kAccCoreRw];
+    unsigned long long cnt = 0;
+    if (K && rw <= rw_max) {
+        const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+        uint32_t *B = smem + (size_t)warp * core_region_words(rw_max);
+        uint32_t *cj = B + rw_max, *cr = cj + 32, *cl = cr + 32;
+        for (uint32_t q = lane; q < rw; q += 32) B[q] = 0u;  // kept all-zero between rows
+        __syncwarp();
+        const uint32_t le = 0xFFFFFFFFu >> (31 - lane);  // lanes 0..lane
+        const uint32_t lt = (1u << lane) - 1u;           // lanes below this one
+        while (true) {
+            unsigned long long k = 0;
+            if (lane == 0) k = atomicAdd(&acc[kAccCoreQ], 1ull);
+            k = __shfl_sync(kFull, k, 0);
+            if (k >= K) break;
+            const uint32_t r = (uint32_t)k;
+            const uint64_t ou = off[c0 + r];
+            const uint32_t d = (uint32_t)(off[c0 + r + 1] - ou);
+            if (d < 2) continue;
+            const uint2 su = __ldg(span + r);  // words of N+(u)
+            if (kChecked && (su.x > su.y || su.y >= rw)) {
+                if (lane == 0) atomicExch(status, kStatusBadForm);
+                continue;
+            }
+            const uint32_t rwg = rw / kCoreGroupWords;  // groups per row, a power of two
+            const uint4 *M4 = reinterpret_cast<const uint4 *>(core_m);
+            uint4 *B4 = reinterpret_cast<uint4 *>(B);
+            const uint32_t gu0 = su.x / kCoreGroupWords, gu1 = su.y / kCoreGroupWords;  // N+(u)
+            for (uint32_t j = gu0 * kCoreVec + lane; j < (gu1 + 1) * kCoreVec; j += 32)
+                B4[j] = __ldg(M4 + (size_t)r * (rw / 4) + j);
+            __syncwarp();
+            uint32_t part = 0;
+            for (uint32_t kb = 0; kb + 1 < d; kb += 32) {
+                const uint32_t i = kb + lane;
+                uint32_t jlo = 1, jhi = 0, vr = 0;
+                if (i + 1 < d) {
+                    vr = __ldg(adj + ou + i) - c0;
+                    if (kChecked && vr >= K) {
+                        atomicExch(status, kStatusBadForm);
+                    } else {
+                        const uint2 sv = __ldg(span + vr);
+                        if (sv.x <= sv.y) {  // groups of N+(v) up to u's last group
+                            jlo = sv.x / kCoreGroupWords;
+                            jhi = min(sv.y / kCoreGroupWords, gu1);
+                        }
+                    }
+                }
+                const uint32_t len = jhi >= jlo ? jhi - jlo + 1 : 0u;
+                const unsigned Z = __ballot_sync(kFull, len != 0);
+                if (!Z) continue;
+                if (len) {
+                    const uint32_t c = __popc(Z & lt);
+                    cj[c] = jlo;
+                    cr[c] = vr;
+                    cl[c] = len;
+                }
+                __syncwarp();
+                const uint32_t nz = __popc(Z);
+                uint32_t sj = 0, sr = 0, sl = 0;
+                if ((uint32_t)lane < nz) {
+                    sj = cj[lane];
+                    sr = cr[lane];
+                    sl = cl[lane];
+                }
+                __syncwarp();
+                uint32_t inc = sl;
+#pragma unroll
+                for (int o = 1; o < 32; o <<= 1) {
+                    const uint32_t t = __shfl_up_sync(kFull, inc, o);
+                    if (lane >= o) inc += t;
+                }
+                const uint32_t T = __shfl_sync(kFull, inc, 31);
+                const uint32_t P = inc - sl;             // first position of this lane's segment
+                const uint32_t dM = sr * rwg + sj - P;   // matrix group of position q: q + dM
+                uint32_t dP = (uint32_t)lane < nz ? P : 0x80000000u;
+                uint32_t before = 0;  // segments starting before the window
+                for (uint32_t t0 = 0; t0 < T; t0 += 32 * kCoreWin) {
+                    uint4 x[kCoreWin][kCoreVec], y[kCoreWin][kCoreVec];
+#pragma unroll
+                    for (int w = 0; w < kCoreWin; ++w) {
+                        const uint32_t Mk = __reduce_or_sync(kFull, bit_or_zero(dP));
+                        const uint32_t eL = (before + __popc(Mk & le) - 1) & 31u;
+                        const uint32_t g = t0 + 32 * w + lane + __shfl_sync(kFull, dM, eL);
+                        const uint32_t gb = g & (rwg - 1);  // the group within the row
+#pragma unroll
+                        for (uint32_t c = 0; c < kCoreVec; ++c) {
+                            x[w][c] = make_uint4(0u, 0u, 0u, 0u);
+                            y[w][c] = x[w][c];
+                        }
+                        if (t0 + 32 * w + lane < T) {
+#pragma unroll
+                            for (uint32_t c = 0; c < kCoreVec; ++c) {
+                                x[w][c] = __ldg(M4 + (size_t)g * kCoreVec + c);
+                                y[w][c] = B4[gb * kCoreVec + c];
+                            }
+                        }
+                        before += __popc(Mk);
+                        dP -= 32;
+                    }
+#pragma unroll
+                    for (int w = 0; w < kCoreWin; ++w)
+#pragma unroll
+                        for (uint32_t c = 0; c < kCoreVec; ++c)
+                            part += __popc(x[w][c].x & y[w][c].x) + __popc(x[w][c].y & y[w][c].y) +
+                                    __popc(x[w][c].z & y[w][c].z) + __popc(x[w][c].w & y[w][c].w);
+                }
+            }
+            cnt += part;
+            __syncwarp();
+            for (uint32_t j = gu0 * kCoreVec + lane; j < (gu1 + 1) * kCoreVec; j += 32)
+                B4[j] = make_uint4(0u, 0u, 0u, 0u);
+            __syncwarp();
+        }
+    }
+    block_add_total(cnt, &acc[0], red);
+}
+
 }  // namespace
 
 struct TcPlan {
@@ -526,9 +809,13 @@ struct TcPlan {
     cudaGraphExec_t exec = nullptr;
     uint64_t *items = nullptr;
     uint32_t *vcnt = nullptr;
+    uint32_t *sdeg = nullptr;     // streamed in-edges per vertex
     void *cub_tmp = nullptr;
     unsigned long long *acc = nullptr;
-    cudaEvent_t k0 = nullptr, k1 = nullptr;
+    uint32_t *core_m = nullptr;   // dense-core matrix and row spans (sized for the largest K)
+    uint2 *core_span = nullptr;
+    uint32_t core_ranks = 0;      // the K picked when the items were built
+    cudaEvent_t k0 = nullptr, k1 = nullptr, c0 = nullptr;
     uint64_t graph_kernels = 0;
     // plain
     uint8_t *bucket = nullptr;
@@ -544,6 +831,9 @@ void tc_plan_free(TcPlan *p) {
     if (p->graph) cudaGraphDestroy(p->graph);
     dev_free(p->items);
     dev_free(p->vcnt);
+    dev_free(p->sdeg);
+    dev_free(p->core_m);
+    dev_free(p->core_span);
     dev_free(p->cub_tmp);
     dev_free(p->acc);
     dev_free(p->bucket);
@@ -551,6 +841,7 @@ void tc_plan_free(TcPlan *p) {
     dev_free(p->bitems);
     if (p->k0) cudaEventDestroy(p->k0);
     if (p->k1) cudaEventDestroy(p->k1);
+    if (p->c0) cudaEventDestroy(p->c0);
     for (auto ev : p->bev)
         if (ev) cudaEventDestroy(ev);
     delete p;
@@ -574,7 +865,8 @@ rtg_config effective_config(const rtg_ctx *ctx, uint64_t m) {
 
 bool same_tc_config(const rtg_config &a, const rtg_config &b) {
     return a.tc_item_edges == b.tc_item_edges && a.tc_region_words == b.tc_region_words &&
-           a.tc_block_warps == b.tc_block_warps && a.tc_blocks_per_sm == b.tc_blocks_per_sm;
+           a.tc_block_warps == b.tc_block_warps && a.tc_blocks_per_sm == b.tc_blocks_per_sm &&
+           a.tc_core_ranks == b.tc_core_ranks;
 }
 
 // Launch shape of the batched count of one graph under one schedule.
@@ -585,7 +877,14 @@ struct BatchedShape {
     int grid, g1;
     uint64_t item_cap;
     size_t cub_bytes;
+    // dense core: the schedule's setting, the largest K it can pick, that K's row words
+    uint32_t core_forced, core_max, core_rw;
+    size_t core_rows_smem, core_smem;
+    int core_rows_grid, core_grid;
+    uint64_t core_m_words() const { return (uint64_t)core_max * core_rw; }
 };
+
+constexpr int kCoreWarps = 8;  // warps per block of both core kernels
 
 rtg_status batched_shape(rtg_ctx *ctx, const CountCsr &c, const rtg_config &cfg,
                          BatchedShape *bs) {
@@ -613,57 +912,126 @@ rtg_status batched_shape(rtg_ctx *ctx, const CountCsr &c, const rtg_config &cfg,
     bs->grid = ctx->sm_count * per_sm;
     bs->g1 = (int)std::max<uint64_t>(1, std::min<uint64_t>((c.n + 256ull) / 256,
                                                           ctx->sm_count * 16ull));
+    bs->core_forced = cfg.tc_core_ranks;
+    bs->core_max = core_max_ranks(cfg.tc_core_ranks, c.n);
+    bs->core_rw = core_row_words(bs->core_max);
+    bs->core_rows_smem = (size_t)kCoreWarps * bs->core_rw * 4;
+    bs->core_smem = (size_t)kCoreWarps * core_region_words(bs->core_rw) * 4;
+    bs->core_rows_grid = bs->core_grid = 1;
+    if (bs->core_max) {
+        if (bs->core_smem + 512 > (size_t)ctx->smem_optin)
+            return fail(ctx, RTG_ERR_INVALID_ARG, "core of %u ranks needs %zu B of shared memory",
+                        bs->core_max, bs->core_smem);
+        RTG_CUDA(ctx, cudaFuncSetAttribute(k_core_rows, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                           (int)bs->core_rows_smem));
+        RTG_CUDA(ctx, cudaFuncSetAttribute(k_tc_core, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                           (int)bs->core_smem));
+        int core_per_sm = 0;
+        RTG_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&core_per_sm, k_tc_core,
+                                                                    kCoreWarps * 32, bs->core_smem));
+        bs->core_grid = ctx->sm_count * std::max(core_per_sm, 1);
+        bs->core_rows_grid = (int)std::max<uint64_t>(
+            1, std::min<uint64_t>((bs->core_max + kCoreWarps - 1) / kCoreWarps, ctx->sm_count * 8ull));
+    }
     return RTG_OK;
 }
 
-// reset -> item counts -> scan -> item fill (acc[2] = number of items)
-void enqueue_items(cudaStream_t st, const CountCsr &c, const BatchedShape &bs, uint64_t *items,
-                   uint32_t *vcnt, void *cub_tmp, unsigned long long *acc) {
-    uint32_t *vbase = vcnt + (c.n + 1ull);
+// Device buffers of one batched count (a plan's, or carved from caller scratch).
+struct CountBufs {
+    uint64_t *items;
+    uint32_t *vcnt;  // 2 (n + 1): items per vertex, their exclusive scan
+    uint32_t *sdeg;  // n + 1
+    void *cub_tmp;
+    unsigned long long *acc;  // kAccWords
+    uint32_t *core_m;         // core_max x core_rw words
+    uint2 *core_span;         // core_max
+};
+
+// reset -> core pick -> item counts (and sdeg) -> scan -> item fill (acc[2] = items)
+void enqueue_items(cudaStream_t st, const CountCsr &c, const BatchedShape &bs, const CountBufs &b) {
+    uint32_t *vbase = b.vcnt + (c.n + 1ull);
     size_t cub_bytes = bs.cub_bytes;
-    cudaMemsetAsync(acc, 0, 8 * sizeof(unsigned long long), st);
-    k_item_counts<<<bs.g1, 256, 0, st>>>(c.off, c.in_off, c.n, bs.pc.E, vcnt);
-    cub::DeviceScan::ExclusiveSum(cub_tmp, cub_bytes, vcnt, vbase, (int64_t)c.n + 1, st);
-    k_item_fill<<<bs.g1, 256, 0, st>>>(c.off, c.in_off, c.n, bs.pc.E, vbase, items, acc);
+    cudaMemsetAsync(b.acc, 0, kAccWords * sizeof(unsigned long long), st);
+    k_core_pick<<<1, 32, 0, st>>>(c.off, c.n, c.m, bs.core_max ? bs.core_forced : RTG_TC_CORE_NONE,
+                                  b.acc);
+    k_item_counts<<<bs.g1, 256, 0, st>>>(c.off, c.in_off, c.in_rng, c.n, bs.pc.E, b.acc, b.vcnt,
+                                         b.sdeg);
+    cub::DeviceScan::ExclusiveSum(b.cub_tmp, cub_bytes, b.vcnt, vbase, (int64_t)c.n + 1, st);
+    k_item_fill<<<bs.g1, 256, 0, st>>>(c.off, b.sdeg, c.n, bs.pc.E, vbase, b.items, b.acc);
 }
 
-// reset of the total and the queue head (acc[2], the item count, stays) -> [k0] persistent
-// count [k1]
-void enqueue_count(cudaStream_t st, const CountCsr &c, const BatchedShape &bs,
-                   const uint64_t *items, unsigned long long *acc, cudaEvent_t k0, cudaEvent_t k1,
-                   bool external_events) {
-    cudaMemsetAsync(acc, 0, 2 * sizeof(unsigned long long), st);
-    if (k0) {
-        if (external_events) cudaEventRecordWithFlags(k0, st, cudaEventRecordExternal);
-        else cudaEventRecord(k0, st);
-    }
-    k_tc_warp<true><<<bs.grid, bs.W * 32, bs.smem, st>>>(c.off, c.adj, c.in_off, c.in_rng, items, acc,
-                                                   bs.pc);
-    if (k1) {
-        if (external_events) cudaEventRecordWithFlags(k1, st, cudaEventRecordExternal);
-        else cudaEventRecord(k1, st);
-    }
+void record(cudaEvent_t ev, cudaStream_t st, bool external) {
+    if (!ev) return;
+    if (external) cudaEventRecordWithFlags(ev, st, cudaEventRecordExternal);
+    else cudaEventRecord(ev, st);
 }
 
-constexpr uint64_t kBatchedKernels = 5;  // item counts, scan (init + sweep), item fill, count
+// core matrix rows -> core count (both return at once without a core); kCoreKernels launches
+constexpr uint64_t kCoreKernels = 2;
 
-void enqueue_batched(cudaStream_t st, const CountCsr &c, const BatchedShape &bs, uint64_t *items,
-                     uint32_t *vcnt, void *cub_tmp, unsigned long long *acc) {
-    enqueue_items(st, c, bs, items, vcnt, cub_tmp, acc);
-    enqueue_count(st, c, bs, items, acc, nullptr, nullptr, false);
+void enqueue_core(cudaStream_t st, const CountCsr &c, const BatchedShape &bs, const CountBufs &b,
+                  uint32_t *status) {
+    k_core_rows<<<bs.core_rows_grid, kCoreWarps * 32, bs.core_rows_smem, st>>>(
+        c.off, c.adj, b.acc, b.core_m, b.core_span, bs.core_rw, status);
+    k_tc_core<<<bs.core_grid, kCoreWarps * 32, bs.core_smem, st>>>(
+        c.off, c.adj, b.core_m, b.core_span, b.acc, bs.core_rw, status);
+}
+
+// reset of the total and the queue head (acc[2], the item count, and the core fields stay)
+// -> [c0] core stage [k0] persistent count [k1]
+void enqueue_count(cudaStream_t st, const CountCsr &c, const BatchedShape &bs, const CountBufs &b,
+                   cudaEvent_t ec0, cudaEvent_t k0, cudaEvent_t k1, bool external_events) {
+    cudaMemsetAsync(b.acc, 0, 2 * sizeof(unsigned long long), st);
+    record(ec0, st, external_events);
+    if (bs.core_max) enqueue_core(st, c, bs, b, bs.pc.status);
+    record(k0, st, external_events);
+    k_tc_warp<true><<<bs.grid, bs.W * 32, bs.smem, st>>>(c.off, c.adj, c.in_off, c.in_rng, b.sdeg,
+                                                         b.items, b.acc, bs.pc);
+    record(k1, st, external_events);
+}
+
+// core pick, item counts, scan (init + sweep), item fill
+constexpr uint64_t kItemKernels = 5;
+
+uint64_t count_kernels(const BatchedShape &bs) { return 1 + (bs.core_max ? kCoreKernels : 0); }
+
+void enqueue_batched(cudaStream_t st, const CountCsr &c, const BatchedShape &bs, const CountBufs &b) {
+    enqueue_items(st, c, bs, b);
+    enqueue_count(st, c, bs, b, nullptr, nullptr, nullptr, false);
 }
 
 // A plan's items, built once when the plan is made (the counting form does not change while
 // the plan exists), so that a replay launches only the count. Ordering them heaviest first
 // by an estimated cost (elements streamed per item) was tried: 2.76 ms on R-MAT-21 against
 // 2.72 ms for descending rank order, which keeps the items of one vertex together.
+CountBufs plan_bufs(const TcPlan *p) {
+    return CountBufs{p->items, p->vcnt, p->sdeg, p->cub_tmp, p->acc, p->core_m, p->core_span};
+}
+
 rtg_status plan_items(rtg_ctx *ctx, const CountCsr &c, const BatchedShape &bs, TcPlan *p) {
-    enqueue_items(ctx->stream, c, bs, p->items, p->vcnt, p->cub_tmp, p->acc);
-    ctx->launches += kBatchedKernels - 1;
+    enqueue_items(ctx->stream, c, bs, plan_bufs(p));
+    ctx->launches += kItemKernels;
     RTG_CUDA(ctx, cudaGetLastError());
     // the plan may be replayed on another context's stream (the serving engine's runs
     // share a graph's plan): the items must be complete before the plan is handed out
+    unsigned long long K = 0;
+    RTG_CUDA(ctx, cudaMemcpyAsync(&K, p->acc + kAccCoreK, 8, cudaMemcpyDeviceToHost, ctx->stream));
     RTG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    p->core_ranks = (uint32_t)K;
+    return RTG_OK;
+}
+
+// plan buffers shared by the BATCHED and BUCKETED plans
+rtg_status alloc_count_bufs(rtg_ctx *ctx, const CountCsr &c, const BatchedShape &bs, TcPlan *p) {
+    RTG_TRY(dev_alloc(ctx, (void **)&p->items, bs.item_cap * 8));
+    RTG_TRY(dev_alloc(ctx, (void **)&p->vcnt, (c.n + 1ull) * 4 * 2));
+    RTG_TRY(dev_alloc(ctx, (void **)&p->sdeg, (c.n + 1ull) * 4));
+    RTG_TRY(dev_alloc(ctx, (void **)&p->acc, kAccWords * sizeof(unsigned long long)));
+    RTG_TRY(dev_alloc(ctx, &p->cub_tmp, bs.cub_bytes));
+    if (bs.core_max) {
+        RTG_TRY(dev_alloc(ctx, (void **)&p->core_m, bs.core_m_words() * 4));
+        RTG_TRY(dev_alloc(ctx, (void **)&p->core_span, (uint64_t)bs.core_max * 8));
+    }
     return RTG_OK;
 }
 
@@ -688,20 +1056,24 @@ rtg_status batched_plan(rtg_ctx *ctx, rtg_graph *g, TcPlan **out) {
     BatchedShape bs{};
     rtg_status s;
     if ((s = batched_shape(ctx, c, cfg, &bs)) != RTG_OK) return bail(s);
-    if ((s = dev_alloc(ctx, (void **)&p->items, bs.item_cap * 8)) != RTG_OK) return bail(s);
-    if ((s = dev_alloc(ctx, (void **)&p->vcnt, (c.n + 1ull) * 4 * 2)) != RTG_OK) return bail(s);
-    if ((s = dev_alloc(ctx, (void **)&p->acc, 8 * sizeof(unsigned long long))) != RTG_OK)
-        return bail(s);
-    if ((s = dev_alloc(ctx, &p->cub_tmp, bs.cub_bytes)) != RTG_OK) return bail(s);
+    if ((s = alloc_count_bufs(ctx, c, bs, p)) != RTG_OK) return bail(s);
     cudaError_t e;
     if ((e = cudaEventCreate(&p->k0)) != cudaSuccess ||
-        (e = cudaEventCreate(&p->k1)) != cudaSuccess)
+        (e = cudaEventCreate(&p->k1)) != cudaSuccess ||
+        (e = cudaEventCreate(&p->c0)) != cudaSuccess)
         return bail(cuda_fail(ctx, e, "event", __FILE__, __LINE__));
     if ((s = plan_items(ctx, c, bs, p)) != RTG_OK) return bail(s);
+    if (!p->core_ranks && bs.core_max) {  // the pick found no core: the graph leaves it out
+        dev_free(p->core_m);
+        dev_free(p->core_span);
+        p->core_m = nullptr;
+        p->core_span = nullptr;
+        bs.core_max = 0;
+    }
     if ((e = cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal)) !=
         cudaSuccess)
         return bail(cuda_fail(ctx, e, "capture", __FILE__, __LINE__));
-    enqueue_count(ctx->stream, c, bs, p->items, p->acc, p->k0, p->k1, true);
+    enqueue_count(ctx->stream, c, bs, plan_bufs(p), p->c0, p->k0, p->k1, true);
     e = cudaStreamEndCapture(ctx->stream, &p->graph);
     if (e != cudaSuccess) return bail(cuda_fail(ctx, e, "end capture", __FILE__, __LINE__));
     if ((e = cudaGraphInstantiate(&p->exec, p->graph, 0)) != cudaSuccess)
@@ -733,12 +1105,15 @@ rtg_status count_batched(rtg_ctx *ctx, rtg_graph *g, uint64_t *total, rtg_timing
     RTG_CUDA(ctx, cudaEventSynchronize(ctx->ev[2]));
     RTG_TRY(check_status_word(ctx));
     *total = h;
-    float ms = 0, kms = 0, dms = 0;
+    float ms = 0, kms = 0, dms = 0, cms = 0;
     cudaEventElapsedTime(&ms, ctx->ev[0], ctx->ev[1]);
     cudaEventElapsedTime(&kms, p->k0, p->k1);
+    cudaEventElapsedTime(&cms, p->c0, p->k0);
     cudaEventElapsedTime(&dms, ctx->ev[1], ctx->ev[2]);
     t->count_ms = ms;
     t->main_kernel_ms = kms;
+    t->core_ms = p->core_ranks ? cms : 0.0;
+    t->core_ranks = p->core_ranks;
     t->d2h_ms += dms;
     t->kernel_launches += p->graph_kernels;
     return RTG_OK;
@@ -838,17 +1213,20 @@ rtg_status count_bucketed(rtg_ctx *ctx, rtg_graph *g, uint64_t *total, rtg_timin
     dcfg.tc_item_edges = c.m >= kLargeItemsFrom ? kLargeItemEdges : kDefaultItemEdges;
     dcfg.tc_block_warps = kDefaultBlockWarps;
     dcfg.tc_region_words = kDefaultRegionWords;
+    dcfg.tc_core_ranks = ctx->cfg.tc_core_ranks;  // the core is the algorithm's, not the schedule's
     BatchedShape bs{};
     RTG_TRY(batched_shape(ctx, c, dcfg, &bs));
     TcPlan *p = g->plan_bucketed;
+    if (p && !same_tc_config(p->cfg, dcfg)) {  // buffers sized for another core setting
+        tc_plan_free(p);
+        p = g->plan_bucketed = nullptr;
+    }
     if (!p) {
         p = new TcPlan();
         p->mode = RTG_TC_BUCKETED;
-        rtg_status s = dev_alloc(ctx, (void **)&p->items, bs.item_cap * 8);
+        p->cfg = dcfg;
+        rtg_status s = alloc_count_bufs(ctx, c, bs, p);
         if (s == RTG_OK) s = dev_alloc(ctx, (void **)&p->bitems, bs.item_cap * 8 * kItemBuckets);
-        if (s == RTG_OK) s = dev_alloc(ctx, (void **)&p->vcnt, (c.n + 1ull) * 4 * 2);
-        if (s == RTG_OK) s = dev_alloc(ctx, (void **)&p->acc, 8 * sizeof(unsigned long long));
-        if (s == RTG_OK) s = dev_alloc(ctx, &p->cub_tmp, bs.cub_bytes);
         if (s != RTG_OK) {
             tc_plan_free(p);
             return s;
@@ -858,19 +1236,32 @@ rtg_status count_bucketed(rtg_ctx *ctx, rtg_graph *g, uint64_t *total, rtg_timin
     RTG_CUDA(ctx, cudaFuncSetAttribute(k_tc_warp<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        (int)bs.smem));
     const uint64_t l0 = ctx->launches;
+    const CountBufs b = plan_bufs(p);
     unsigned long long *acc = p->acc, *bcnt = p->acc + 3;
     RTG_CUDA(ctx, cudaEventRecord(ctx->ev[0], ctx->stream));
-    enqueue_items(ctx->stream, c, bs, p->items, p->vcnt, p->cub_tmp, acc);  // zeroes acc[0..7]
-    ctx->launches += kBatchedKernels - 1;
+    enqueue_items(ctx->stream, c, bs, b);  // zeroes acc
+    ctx->launches += kItemKernels;
     const int gb = (int)std::max<uint64_t>(1, std::min<uint64_t>((bs.item_cap + 255) / 256,
                                                                   ctx->sm_count * 16ull));
-    k_item_bucket<<<gb, 256, 0, ctx->stream>>>(p->items, acc + 2, c.in_off, bs.pc.E, bs.item_cap,
+    k_item_bucket<<<gb, 256, 0, ctx->stream>>>(p->items, acc + 2, p->sdeg, bs.pc.E, bs.item_cap,
                                                p->bitems, bcnt);
     ctx->launches++;
     RTG_CUDA(ctx, cudaGetLastError());
-    unsigned long long hc[kItemBuckets] = {0};
+    float cms = 0;
+    if (bs.core_max) {
+        RTG_CUDA(ctx, cudaEventRecord(ctx->ev[4], ctx->stream));
+        enqueue_core(ctx->stream, c, bs, b, ctx->d_status);
+        ctx->launches += kCoreKernels;
+        RTG_CUDA(ctx, cudaGetLastError());
+        RTG_CUDA(ctx, cudaEventRecord(ctx->ev[5], ctx->stream));
+    }
+    // bucket counts (acc[3..5]) and the core's size (acc[8])
+    unsigned long long hc[kAccCoreK - 2] = {0};
     RTG_CUDA(ctx, cudaMemcpyAsync(hc, bcnt, sizeof hc, cudaMemcpyDeviceToHost, ctx->stream));
     RTG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    if (bs.core_max) cudaEventElapsedTime(&cms, ctx->ev[4], ctx->ev[5]);
+    t->core_ranks = (uint32_t)hc[kAccCoreK - 3];
+    t->core_ms = t->core_ranks ? cms : 0.0;
     float kms_sum = 0;
     for (int r = 0; r < kItemBuckets; ++r) {
         if (!hc[r]) continue;
@@ -880,7 +1271,7 @@ rtg_status count_bucketed(rtg_ctx *ctx, rtg_graph *g, uint64_t *total, rtg_timin
         const uint64_t blocks = (hc[r] + bs.W - 1) / bs.W;
         RTG_CUDA(ctx, cudaEventRecord(ctx->ev[4], ctx->stream));
         k_tc_warp<false><<<(unsigned)blocks, bs.W * 32, bs.smem, ctx->stream>>>(
-            c.off, c.adj, c.in_off, c.in_rng, p->bitems + r * bs.item_cap, acc, pc);
+            c.off, c.adj, c.in_off, c.in_rng, p->sdeg, p->bitems + r * bs.item_cap, acc, pc);
         ctx->launches++;
         RTG_CUDA(ctx, cudaGetLastError());
         RTG_CUDA(ctx, cudaEventRecord(ctx->ev[5], ctx->stream));
@@ -910,8 +1301,11 @@ rtg_status count_bucketed(rtg_ctx *ctx, rtg_graph *g, uint64_t *total, rtg_timin
 uint64_t tc_plan_estimate_bytes(const rtg_ctx *ctx, const rtg_graph *g) {
     const CountCsr &c = g->cnt;
     const rtg_config cfg = effective_config(ctx, c.m);
-    // items + vertex counts + scan temporary (bounded by one word per vertex) + totals
-    return (c.m / cfg.tc_item_edges + c.n + 1) * 8 + (c.n + 1ull) * 8 + (c.n + 1ull) * 4 + 4096;
+    const uint32_t K = core_max_ranks(cfg.tc_core_ranks, c.n);
+    // items + vertex counts and their scan + sdeg + scan temporary (bounded by one word per
+    // vertex) + totals and alignment + core matrix and spans
+    return (c.m / cfg.tc_item_edges + c.n + 1) * 8 + (c.n + 1ull) * 8 + (c.n + 1ull) * 4 +
+           (c.n + 1ull) * 4 + 4096 + (uint64_t)K * core_row_words(K) * 4 + (uint64_t)K * 8;
 }
 
 rtg_status tc_launch_direct(rtg_ctx *ctx, rtg_graph *g, void *scratch, uint64_t scratch_bytes,
@@ -929,19 +1323,24 @@ rtg_status tc_launch_direct(rtg_ctx *ctx, rtg_graph *g, void *scratch, uint64_t 
     if (kChecked) RTG_TRY(check_count_form(ctx, c));
     BatchedShape bs{};
     RTG_TRY(batched_shape(ctx, c, effective_config(ctx, c.m), &bs));
-    // scratch: acc (64 B) | items | vertex counts and offsets | scan temporary
-    char *p = static_cast<char *>(scratch);
-    unsigned long long *acc = reinterpret_cast<unsigned long long *>(p);
-    uint64_t *items = reinterpret_cast<uint64_t *>(p + 64);
-    uint32_t *vcnt = reinterpret_cast<uint32_t *>(items + bs.item_cap);
-    void *tmp = reinterpret_cast<void *>(
-        (reinterpret_cast<uintptr_t>(vcnt + 2 * (c.n + 1ull)) + 255) & ~(uintptr_t)255);
-    if ((uint64_t)(static_cast<char *>(tmp) - p) + bs.cub_bytes > scratch_bytes)
+    // scratch: acc | core matrix | core spans | items | vertex counts and their scan | sdeg |
+    // scan temporary (the matrix and the scan temporary 256-byte aligned)
+    auto up = [](uintptr_t x) { return (x + 255) & ~(uintptr_t)255; };
+    const uintptr_t p0 = reinterpret_cast<uintptr_t>(scratch);
+    CountBufs b{};
+    b.acc = reinterpret_cast<unsigned long long *>(p0);
+    b.core_m = reinterpret_cast<uint32_t *>(up(p0 + kAccWords * 8));
+    b.core_span = reinterpret_cast<uint2 *>(b.core_m + bs.core_m_words());
+    b.items = reinterpret_cast<uint64_t *>(b.core_span + bs.core_max);
+    b.vcnt = reinterpret_cast<uint32_t *>(b.items + bs.item_cap);
+    b.sdeg = b.vcnt + 2 * (c.n + 1ull);
+    b.cub_tmp = reinterpret_cast<void *>(up(reinterpret_cast<uintptr_t>(b.sdeg + (c.n + 1ull))));
+    if ((uint64_t)(reinterpret_cast<uintptr_t>(b.cub_tmp) - p0) + bs.cub_bytes > scratch_bytes)
         return fail(ctx, RTG_ERR_INVALID_ARG, "scratch too small for the count");
-    enqueue_batched(ctx->stream, c, bs, items, vcnt, tmp, acc);
+    enqueue_batched(ctx->stream, c, bs, b);
     RTG_CUDA(ctx, cudaGetLastError());
-    ctx->launches += kBatchedKernels;
-    RTG_CUDA(ctx, cudaMemcpyAsync(h_total, acc, 8, cudaMemcpyDeviceToHost, ctx->stream));
+    ctx->launches += kItemKernels + count_kernels(bs);
+    RTG_CUDA(ctx, cudaMemcpyAsync(h_total, b.acc, 8, cudaMemcpyDeviceToHost, ctx->stream));
     return RTG_OK;
 }
 

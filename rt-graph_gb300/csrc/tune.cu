@@ -129,6 +129,7 @@ extern "C" rtg_status rtg_tune_tc(rtg_ctx *ctx, rtg_graph *g, const char *cache_
     // the SI fields of the context's schedule are kept as they are
     rtg_config def = saved;
     def.tc_item_edges = def.tc_region_words = def.tc_block_warps = def.tc_blocks_per_sm = 0;
+    def.tc_core_ranks = 0;
     uint64_t want = 0;
     double def_ms = 0;
     rtg_status st = run(def, &want, &def_ms);

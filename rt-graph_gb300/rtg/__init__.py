@@ -27,6 +27,8 @@ OK, ERR_INVALID_ARG, ERR_OOM, ERR_IO, ERR_FORMAT, ERR_DEVICE, ERR_TIMEOUT, ERR_C
 FMT_EDGE_BIN, FMT_EDGE_TXT, FMT_MTX, FMT_RTG_CSR = 0, 1, 2, 3
 ORIENT_DEGREE, ORIENT_DEGREE_RAW_REF, ORIENT_SYMMETRIC = 0, 1, 2
 TC_PLAIN, TC_BATCHED, TC_BUCKETED = 0, 1, 2
+TC_CORE_NONE = 0xFFFFFFFF     # rtg_config.tc_core_ranks: no dense core
+TC_CORE_MAX_RANKS = 32768
 SI_AUTO, SI_MERGE, SI_SEARCH, SI_BITMAP, SI_PLAIN = 0, 1, 2, 3, 4
 PAIRS_DEVICE, OUT_DEVICE = 0x100, 0x200
 
@@ -36,7 +38,8 @@ class Timing(C.Structure):
                 ("main_kernel_ms", C.c_double), ("d2h_ms", C.c_double),
                 ("total_ms", C.c_double), ("kernel_launches", C.c_uint64),
                 ("algo_bytes", C.c_uint64), ("h2d_bytes", C.c_uint64),
-                ("d2h_bytes", C.c_uint64)]
+                ("d2h_bytes", C.c_uint64), ("core_ms", C.c_double),
+                ("core_ranks", C.c_uint32), ("reserved", C.c_uint32)]
 
     def as_dict(self) -> dict:
         return {k: getattr(self, k) for k, _ in self._fields_}
@@ -53,7 +56,7 @@ class Config(C.Structure):
     _fields_ = [(k, C.c_uint32) for k in (
         "tc_block_warps", "tc_item_edges", "tc_region_words", "tc_blocks_per_sm",
         "si_block_warps", "si_search_ratio", "si_stage_slots", "si_stage_bytes",
-        "si_blocks_per_sm", "si_skew_stream", "si_form")]
+        "si_blocks_per_sm", "si_skew_stream", "si_form", "tc_core_ranks")]
 
     def as_dict(self) -> dict:
         return {k: getattr(self, k) for k, _ in self._fields_}

@@ -106,4 +106,12 @@ def forgeries(form) -> dict:
     v = _row_with(in_off, 1)
     io[v], io[v + 1] = io[v + 1], io[v]
     out["in-edge offsets out of order"] = (n, off, adj, io, rng)
+    # two in-edges of one head swapped: every range still valid, the source order broken
+    r = rng.copy()
+    first = in_off[:-1].astype(np.int64)
+    k = int(np.nonzero((np.diff(in_off.astype(np.int64)) >= 2) &
+                       (r[np.minimum(first + 1, len(r) - 1), 0] > r[first, 0]))[0][0])
+    e = int(in_off[k])
+    r[[e, e + 1]] = r[[e + 1, e]]
+    out["in-edges out of source order"] = (n, off, adj, in_off, r)
     return out

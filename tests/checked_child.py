@@ -1,7 +1,8 @@
 """Child process of tests/test_checked_gpu.py: runs against the library named by RTG_LIB
 (the checked build) and exits non-zero on any mismatch.
 
-  parity  – triangle counts of golden graphs in every form, batched set intersections in
+  parity  – triangle counts of golden graphs in every form (the batched forms also with a
+            forced dense core), batched set intersections in
             both kernel forms and one serving round (a count and a pair batch), against the
             golden counts and the oracle
   forged  – counting forms forged to break one invariant each, loaded past the host-side
@@ -37,6 +38,13 @@ def parity() -> None:
             for mode in (rtg.TC_PLAIN, rtg.TC_BATCHED, rtg.TC_BUCKETED):
                 got, _ = g.tc(mode)
                 assert got == rec["triangles"], (name, mode, got)
+            saved = ctx.config().as_dict()
+            for K in (100, 32768):  # dense-core stage, checked kernels
+                ctx.set_config(**dict(saved, tc_core_ranks=K))
+                for mode in (rtg.TC_BATCHED, rtg.TC_BUCKETED):
+                    got, t = g.tc(mode)
+                    assert got == rec["triangles"] and t.core_ranks, (name, K, mode, got)
+            ctx.set_config(**saved)
             g.close()
         s, d = rtg.gen_rmat(14, 16, seed=2)
         got, _ = ctx.tc_count_host_edges(s, d, rtg.ORIENT_DEGREE, rtg.TC_BATCHED)

@@ -158,3 +158,39 @@ def test_checked_build_variant_loads_and_flags_itself():
     assert checked.rtg_checked_build() == 1
     assert checked.rtg_debug_skip_file_checks(1) == rtg.OK
     assert checked.rtg_debug_skip_file_checks(0) == rtg.OK
+
+
+def test_struct_layouts_match_the_header(tmp_path):
+    """The ctypes mirrors of the public structs have the header's size and field offsets
+    (a C program built with gcc against include/rtg.h prints them)."""
+    import ctypes as C
+    structs = {"rtg_config": rtg.Config, "rtg_timing": rtg.Timing,
+               "rtg_graph_info": rtg.GraphInfo, "rtg_tune_result": rtg.TuneResult}
+    lines = ['#include <stdio.h>', '#include <stddef.h>', '#include "rtg.h"', 'int main(void) {']
+    for cname, py in structs.items():
+        lines.append(f'printf("{cname} sizeof %zu\\n", sizeof({cname}));')
+        for f, _ in py._fields_:
+            lines.append(f'printf("{cname} {f} %zu\\n", offsetof({cname}, {f}));')
+    lines += ['return 0;', '}']
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines) + "\n")
+    exe = tmp_path / "layout"
+    subprocess.run(["gcc", "-std=c11", "-I", str(REPO / "include"), str(src), "-o", str(exe)],
+                   check=True)
+    got = {}
+    for line in subprocess.run([str(exe)], check=True, capture_output=True,
+                               text=True).stdout.splitlines():
+        s, f, v = line.split()
+        got[(s, f)] = int(v)
+    for cname, py in structs.items():
+        assert got[(cname, "sizeof")] == C.sizeof(py), cname
+        for f, _ in py._fields_:
+            assert got[(cname, f)] == getattr(py, f).offset, (cname, f)
+
+
+def test_core_config_constants():
+    assert rtg.TC_CORE_NONE == 0xFFFFFFFF
+    assert rtg.TC_CORE_MAX_RANKS == 32768
+    text = (REPO / "include" / "rtg.h").read_text()
+    assert "#define RTG_TC_CORE_NONE 0xFFFFFFFFu" in text
+    assert "#define RTG_TC_CORE_MAX_RANKS 32768u" in text

@@ -45,14 +45,23 @@ def six():
 
 
 @pytest.mark.parametrize("orient", [rtg.ORIENT_DEGREE, rtg.ORIENT_DEGREE_RAW_REF])
-def test_every_six_vertex_graph_total(ctx, six, orient):
+@pytest.mark.parametrize("core", [0, 7, 32768, rtg.TC_CORE_NONE])
+def test_every_six_vertex_graph_total(ctx, six, orient, core):
+    """core: the dense-core size of the batched forms (a core of 7 or 32768 top ranks cuts
+    through small graphs, so their triangles are split between the core count and the
+    streamed in-edges)."""
     s, d, tri = six
     g = ctx.graph_from_edges(s, d).build(orient)
-    for mode in (rtg.TC_PLAIN, rtg.TC_BATCHED, rtg.TC_BUCKETED):
-        got, _ = g.tc(mode)
-        assert got == int(tri.sum()), mode
-    got, _ = ctx.tc_count_host_edges(s, d, rtg.ORIENT_DEGREE, rtg.TC_BATCHED)
-    assert got == int(tri.sum())
+    saved = ctx.config().as_dict()
+    try:
+        ctx.set_config(**dict(saved, tc_core_ranks=core))
+        for mode in (rtg.TC_PLAIN, rtg.TC_BATCHED, rtg.TC_BUCKETED):
+            got, _ = g.tc(mode)
+            assert got == int(tri.sum()), mode
+        got, _ = ctx.tc_count_host_edges(s, d, rtg.ORIENT_DEGREE, rtg.TC_BATCHED)
+        assert got == int(tri.sum())
+    finally:
+        ctx.set_config(**saved)
     g.close()
 
 
