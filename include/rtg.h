@@ -182,9 +182,10 @@ typedef struct rtg_config {
                                    top min(value, n) ranks (1..32768) have their
                                    adjacency held as a bit matrix, and their edges are
                                    counted by word AND + popcount; RTG_TC_CORE_NONE: no
-                                   core; 0 = library choice (the largest of 16384, 8192,
-                                   4096, 2048, 1024 top ranks whose edge density is at
-                                   least 3 %, none if no such core)                  */
+                                   core; 0 = library choice (the largest of 32768, 24576,
+                                   16384, 12288, 8192, 6144, 4096, 3072, 2048, 1536,
+                                   1024 top ranks whose edge density is at least 2.5 %,
+                                   none if no such core)                             */
 } rtg_config;
 
 #define RTG_TC_CORE_NONE 0xFFFFFFFFu

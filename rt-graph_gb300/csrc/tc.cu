@@ -35,8 +35,8 @@
 //           memory, the word ranges of all its edges swept as one flat sequence), and
 //           streams only the in-edges whose source lies below c0: the in-edges of a head
 //           are ordered by source, so those are the first sdeg[v] of them. K is picked on
-//           the device from the offsets when the items are built (the largest of 16384 ..
-//           1024 top ranks with edge density >= 3 %, or none), or set by the schedule.
+//           the device from the offsets when the items are built (the largest of 32768 ..
+//           1024 top ranks with edge density >= 2.5 %, or none), or set by the schedule.
 //           The items are built once per (graph, schedule); the count (counter resets,
 //           core matrix, core count, the persistent kernel) is one CUDA graph, captured
 //           once and replayed. uint64 totals: lane partials -> warp shuffle sum -> block
@@ -173,12 +173,21 @@ __global__ void __launch_bounds__(256) k_plain_edges(const uint64_t *__restrict_
 constexpr int kAccWords = 16;
 constexpr int kAccCoreQ = 6, kAccCoreK = 8, kAccCoreC0 = 9, kAccCoreRw = 10, kAccCoreXc = 11;
 
-// Core sizes the library picks from, and the edge density (per cent of K (K - 1) / 2) the
-// core must reach. Measured on R-MAT scale 18/20/21 (edge factor 16): the largest core of at
-// least 3 % density removes 40-55 % of the element work (cost model: 7 instructions per
-// streamed element, 5 per word of AND); on Holme-Kim and Barabasi-Albert graphs of 2^20
-// vertices no core reaches 2 %, and a 16K core there would add work.
-constexpr uint32_t kCoreAutoMax = 16384, kCoreAutoMin = 1024, kCoreMinDensityPct = 3;
+// Core sizes the library picks from (largest first), and the edge density the core must
+// reach (per mille of K (K - 1) / 2): the largest candidate at or above it. Cost measured on
+// R-MAT scale 21 (edge factor 16, 16384 and 32768 core ranks): 4.8e-10 ms per streamed
+// element, 3.8e-10 ms per swept matrix word. With those rates the best candidate is the
+// largest of 2.5 % density or more on R-MAT scale 18, 20 and 21 (edge factor 16: 12288,
+// 16384 and 24576 ranks) and within 2 % of the best at edge factor 8 (16384 for 12288); on
+// Holme-Kim and Barabasi-Albert graphs of 2^20 vertices no core reaches 1.5 % and none would
+// pay.
+constexpr int kCoreCandidates = 11;
+constexpr uint32_t kCoreMinDensityPerMille = 25;
+
+// candidate i, largest first: 32768, 24576, 16384, 12288, ..., 1536, 1024
+__host__ __device__ constexpr uint32_t core_candidate(int i) {
+    return (i & 1) ? 24576u >> (i / 2) : 32768u >> (i / 2);
+}
 
 // The core count sweeps the matrix in groups of kCoreGroupWords words (16 bytes, one load per
 // lane and position). Measured on R-MAT scale 21 with 16384 core ranks: 0.25-0.27 ms with
@@ -200,8 +209,8 @@ __host__ __device__ constexpr uint32_t core_row_words(uint32_t K) {
 uint32_t core_max_ranks(uint32_t forced, uint32_t n) {
     if (forced == RTG_TC_CORE_NONE) return 0;
     if (forced) return std::min(forced, n);
-    for (uint32_t c = kCoreAutoMax; c >= kCoreAutoMin; c >>= 1)
-        if (c <= n) return c;
+    for (int i = 0; i < kCoreCandidates; ++i)
+        if (core_candidate(i) <= n) return core_candidate(i);
     return 0;
 }
 
@@ -214,10 +223,11 @@ __global__ void k_core_pick(const uint64_t *__restrict__ off, uint32_t n, uint64
     if (forced == RTG_TC_CORE_NONE) K = 0;
     else if (forced) K = min(forced, n);
     else
-        for (uint32_t c = kCoreAutoMax; c >= kCoreAutoMin; c >>= 1) {
+        for (int i = 0; i < kCoreCandidates; ++i) {
+            const uint32_t c = core_candidate(i);
             if (c > n) continue;
             const uint64_t ce = m - off[n - c];
-            if (100ull * ce >= (uint64_t)kCoreMinDensityPct * c * (c - 1) / 2) {
+            if (1000ull * ce >= (uint64_t)kCoreMinDensityPerMille * c * (c - 1) / 2) {
                 K = c;
                 break;
             }
@@ -656,9 +666,12 @@ __global__ void __launch_bounds__(256) k_core_rows(const uint64_t *__restrict__ 
     }
 }
 
-// Per-warp shared memory of k_tc_core: the staged row (rw_max words) and the compacted
-// segments of a batch of 32 edges (first group, matrix row, length: 3 x 32 words).
-__host__ __device__ constexpr uint32_t core_region_words(uint32_t rw_max) { return rw_max + 96; }
+// Per-warp shared memory of k_tc_core: the staged row (rw_max words), one guard group that
+// stays zero (positions past the end of a sweep read it), and the compacted segments of a
+// batch of 32 edges (first group, matrix row, length: 3 x 32 words).
+__host__ __device__ constexpr uint32_t core_region_words(uint32_t rw_max) {
+    return rw_max + kCoreGroupWords + 96;
+}
 constexpr int kCoreWin = 4;  // 32-position windows whose loads are in flight together
 
 // Core count: warps take core rows r from the queue (acc[kAccCoreQ]), heaviest (lowest rank)
@@ -687,8 +700,10 @@ __global__ void __launch_bounds__(256) k_tc_core(const uint64_t *__restrict__ of
     if (K && rw <= rw_max) {
         const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
         uint32_t *B = smem + (size_t)warp * core_region_words(rw_max);
-        uint32_t *cj = B + rw_max, *cr = cj + 32, *cl = cr + 32;
-        for (uint32_t q = lane; q < rw; q += 32) B[q] = 0u;  // kept all-zero between rows
+        uint32_t *cj = B + rw_max + kCoreGroupWords, *cr = cj + 32, *cl = cr + 32;
+        const uint32_t guard = rw_max / kCoreGroupWords;  // the zero group after the row
+        // all-zero between rows, the guard group always
+        for (uint32_t q = lane; q < rw_max + kCoreGroupWords; q += 32) B[q] = 0u;
         __syncwarp();
         const uint32_t le = 0xFFFFFFFFu >> (31 - lane);  // lanes 0..lane
         const uint32_t lt = (1u << lane) - 1u;           // lanes below this one
@@ -714,11 +729,15 @@ __global__ void __launch_bounds__(256) k_tc_core(const uint64_t *__restrict__ of
                 B4[j] = __ldg(M4 + (size_t)r * (rw / 4) + j);
             __syncwarp();
             uint32_t part = 0;
+            // the batch's heads, loaded one batch ahead
+            uint32_t vnx = (uint32_t)lane + 1 < d ? __ldg(adj + ou + lane) : 0u;
             for (uint32_t kb = 0; kb + 1 < d; kb += 32) {
                 const uint32_t i = kb + lane;
                 uint32_t jlo = 1, jhi = 0, vr = 0;
+                const uint32_t vcur = vnx;
+                vnx = i + 33 < d ? __ldg(adj + ou + i + 32) : 0u;
                 if (i + 1 < d) {
-                    vr = __ldg(adj + ou + i) - c0;
+                    vr = vcur - c0;
                     if (kChecked && vr >= K) {
                         atomicExch(status, kStatusBadForm);
                     } else {
@@ -764,19 +783,17 @@ __global__ void __launch_bounds__(256) k_tc_core(const uint64_t *__restrict__ of
                     for (int w = 0; w < kCoreWin; ++w) {
                         const uint32_t Mk = __reduce_or_sync(kFull, bit_or_zero(dP));
                         const uint32_t eL = (before + __popc(Mk & le) - 1) & 31u;
-                        const uint32_t g = t0 + 32 * w + lane + __shfl_sync(kFull, dM, eL);
-                        const uint32_t gb = g & (rwg - 1);  // the group within the row
+                        const uint32_t q = t0 + 32 * w + lane;
+                        uint32_t g = q + __shfl_sync(kFull, dM, eL);
+                        uint32_t gb = g & (rwg - 1);  // the group within the row
+                        if (q >= T) {  // past the sweep: matrix group 0 against the zero guard
+                            g = 0;
+                            gb = guard;
+                        }
 #pragma unroll
                         for (uint32_t c = 0; c < kCoreVec; ++c) {
-                            x[w][c] = make_uint4(0u, 0u, 0u, 0u);
-                            y[w][c] = x[w][c];
-                        }
-                        if (t0 + 32 * w + lane < T) {
-#pragma unroll
-                            for (uint32_t c = 0; c < kCoreVec; ++c) {
-                                x[w][c] = __ldg(M4 + (size_t)g * kCoreVec + c);
-                                y[w][c] = B4[gb * kCoreVec + c];
-                            }
+                            x[w][c] = __ldg(M4 + (size_t)g * kCoreVec + c);
+                            y[w][c] = B4[gb * kCoreVec + c];
                         }
                         before += __popc(Mk);
                         dP -= 32;
@@ -886,6 +903,30 @@ struct BatchedShape {
 
 constexpr int kCoreWarps = 8;  // warps per block of both core kernels
 
+// The core kernels' buffers and launch shape for cores of at most K ranks.
+rtg_status core_shape(rtg_ctx *ctx, uint32_t K, BatchedShape *bs) {
+    bs->core_max = K;
+    bs->core_rw = core_row_words(K);
+    bs->core_rows_smem = (size_t)kCoreWarps * bs->core_rw * 4;
+    bs->core_smem = (size_t)kCoreWarps * core_region_words(bs->core_rw) * 4;
+    bs->core_rows_grid = bs->core_grid = 1;
+    if (!K) return RTG_OK;
+    if (bs->core_smem + 512 > (size_t)ctx->smem_optin)
+        return fail(ctx, RTG_ERR_INVALID_ARG, "core of %u ranks needs %zu B of shared memory", K,
+                    bs->core_smem);
+    RTG_CUDA(ctx, cudaFuncSetAttribute(k_core_rows, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)bs->core_rows_smem));
+    RTG_CUDA(ctx, cudaFuncSetAttribute(k_tc_core, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)bs->core_smem));
+    int per_sm = 0;
+    RTG_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_tc_core, kCoreWarps * 32,
+                                                                bs->core_smem));
+    bs->core_grid = ctx->sm_count * std::max(per_sm, 1);
+    bs->core_rows_grid = (int)std::max<uint64_t>(
+        1, std::min<uint64_t>((K + kCoreWarps - 1) / kCoreWarps, ctx->sm_count * 8ull));
+    return RTG_OK;
+}
+
 rtg_status batched_shape(rtg_ctx *ctx, const CountCsr &c, const rtg_config &cfg,
                          BatchedShape *bs) {
     bs->W = cfg.tc_block_warps;
@@ -913,27 +954,7 @@ rtg_status batched_shape(rtg_ctx *ctx, const CountCsr &c, const rtg_config &cfg,
     bs->g1 = (int)std::max<uint64_t>(1, std::min<uint64_t>((c.n + 256ull) / 256,
                                                           ctx->sm_count * 16ull));
     bs->core_forced = cfg.tc_core_ranks;
-    bs->core_max = core_max_ranks(cfg.tc_core_ranks, c.n);
-    bs->core_rw = core_row_words(bs->core_max);
-    bs->core_rows_smem = (size_t)kCoreWarps * bs->core_rw * 4;
-    bs->core_smem = (size_t)kCoreWarps * core_region_words(bs->core_rw) * 4;
-    bs->core_rows_grid = bs->core_grid = 1;
-    if (bs->core_max) {
-        if (bs->core_smem + 512 > (size_t)ctx->smem_optin)
-            return fail(ctx, RTG_ERR_INVALID_ARG, "core of %u ranks needs %zu B of shared memory",
-                        bs->core_max, bs->core_smem);
-        RTG_CUDA(ctx, cudaFuncSetAttribute(k_core_rows, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                           (int)bs->core_rows_smem));
-        RTG_CUDA(ctx, cudaFuncSetAttribute(k_tc_core, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                           (int)bs->core_smem));
-        int core_per_sm = 0;
-        RTG_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&core_per_sm, k_tc_core,
-                                                                    kCoreWarps * 32, bs->core_smem));
-        bs->core_grid = ctx->sm_count * std::max(core_per_sm, 1);
-        bs->core_rows_grid = (int)std::max<uint64_t>(
-            1, std::min<uint64_t>((bs->core_max + kCoreWarps - 1) / kCoreWarps, ctx->sm_count * 8ull));
-    }
-    return RTG_OK;
+    return core_shape(ctx, core_max_ranks(cfg.tc_core_ranks, c.n), bs);
 }
 
 // Device buffers of one batched count (a plan's, or carved from caller scratch).
@@ -1063,12 +1084,16 @@ rtg_status batched_plan(rtg_ctx *ctx, rtg_graph *g, TcPlan **out) {
         (e = cudaEventCreate(&p->c0)) != cudaSuccess)
         return bail(cuda_fail(ctx, e, "event", __FILE__, __LINE__));
     if ((s = plan_items(ctx, c, bs, p)) != RTG_OK) return bail(s);
-    if (!p->core_ranks && bs.core_max) {  // the pick found no core: the graph leaves it out
+    if (p->core_ranks != bs.core_max) {  // the buffers shrink to the core the pick chose
         dev_free(p->core_m);
         dev_free(p->core_span);
         p->core_m = nullptr;
         p->core_span = nullptr;
-        bs.core_max = 0;
+        if ((s = core_shape(ctx, p->core_ranks, &bs)) != RTG_OK) return bail(s);
+        if (bs.core_max &&
+            ((s = dev_alloc(ctx, (void **)&p->core_m, bs.core_m_words() * 4)) != RTG_OK ||
+             (s = dev_alloc(ctx, (void **)&p->core_span, (uint64_t)bs.core_max * 8)) != RTG_OK))
+            return bail(s);
     }
     if ((e = cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal)) !=
         cudaSuccess)

@@ -3,9 +3,10 @@
 The top K ranks of the counting form are counted as word ANDs of their adjacency bit
 matrix and the remaining in-edges are streamed; the sum must equal the golden count for
 every core size, from a single rank to the whole graph, in the BATCHED (plan + CUDA graph),
-BUCKETED and one-shot (caller scratch) paths. The library's own choice is checked on
-graphs far from its density bar: R-MAT scale 18 (top 8192 ranks 4.3 % dense, top 16384
-1.6 %) and Holme-Kim 2^20 (no core above 1.5 %).
+BUCKETED and one-shot (caller scratch) paths. The library's own choice (the largest
+candidate core of at least 2.5 % edge density) is checked on graphs far from that bar:
+R-MAT scale 20 (top 16384 ranks 3.6 % dense, top 24576 2.1 %) and Holme-Kim 2^20 (no
+core above 1.5 %).
 """
 from __future__ import annotations
 
@@ -88,15 +89,17 @@ def test_dense_random_graph_whole_core(ctx):
 
 
 def test_library_choice(ctx):
-    s, d = rtg.gen_rmat(18, 16, 0.57, 0.19, 0.19, seed=42)
+    s, d = rtg.gen_rmat(20, 16, 0.57, 0.19, 0.19, seed=42)
     g = ctx.graph_from_edges(s, d).build(rtg.ORIENT_DEGREE)
     off, adj = g.csr()
     want = oracle.tc_merge(off, adj)
     with core_config(ctx, tc_core_ranks=0):
         got, t = g.tc(rtg.TC_BATCHED)
-        assert (got, t.core_ranks) == (want, 8192)
+        assert (got, t.core_ranks) == (want, 16384)
         got, t = g.tc(rtg.TC_BUCKETED)
-        assert (got, t.core_ranks) == (want, 8192)
+        assert (got, t.core_ranks) == (want, 16384)
+        got, _ = ctx.tc_count_host_edges(s, d, rtg.ORIENT_DEGREE, rtg.TC_BATCHED)
+        assert got == want
     with core_config(ctx, tc_core_ranks=rtg.TC_CORE_NONE):
         got, t = g.tc(rtg.TC_BATCHED)
         assert (got, t.core_ranks, t.core_ms) == (want, 0, 0.0)
