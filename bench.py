@@ -5,20 +5,25 @@ Workload (the batched-TC configuration): R-MAT scale 21, edge factor 16 (2^25 sa
 (a,b,c,d) = (0.57,0.19,0.19,0.05), seed 42, symmetrised, deduplicated, self loops removed,
 oriented by degree. A step is one exact uint64 count of the resident CSR:
 
-  value   – edges/s = m / device time of the BATCHED count (persistent kernel in a CUDA
-            graph), CSR resident in HBM, L2 flushed before every step (CUDA events).
+  value   – edges/s = m / device time of the BATCHED count (dense-core stage + persistent
+            streaming kernel in one CUDA graph), CSR resident in HBM, L2 flushed before
+            every step (CUDA events).
   e2e     – the same metric through the public C ABI with host buffers:
             rtg_tc_count_host_edges (pinned host edges -> H2D -> GPU CSR build -> count ->
             D2H of the total), wall time per call.
   plain   – the PLAIN form (one launch per bucket, one warp per oriented edge, the
             reference's per-edge formulation) on the same CSR, for the batched/plain ratio.
-  roofline– the persistent kernel's own algorithmic bytes per launch (4 B per streamed
-            suffix element, 8 B per in-edge range, 4 B per out-list element marked, 16 B of
-            offsets per vertex) over its CUDA-event duration against the measured HBM copy
-            peak; beside it the per-edge work formula of the measurement plan
-            (4 x sum over oriented edges of (d+(u) + d+(v)) + 8 m) as a work-equivalent
-            rate, and the DRAM traffic, issue activity and instructions per element from
-            the committed ncu summary of the same kernel.
+  roofline– the persistent streaming kernel's own algorithmic bytes per launch (4 B per
+            streamed suffix element, 8 B per streamed in-edge range, 4 B per out-list element
+            marked, 16 B of offsets per vertex; only in-edges whose source lies below the
+            dense core are streamed) over its CUDA-event duration against the measured HBM
+            copy peak; beside it the per-edge work formula of the measurement plan
+            (4 x sum over oriented edges of (d+(u) + d+(v)) + 8 m) over the whole count as a
+            work-equivalent rate, and the DRAM traffic, issue activity and instructions per
+            element from the committed ncu summary of the same kernel.
+  core    – the dense-core stage of the same count: its top ranks, device time (matrix
+            build + word-AND count), core edges, matrix bytes, and the 16-byte groups the
+            core count sweeps (each read from L2 and ANDed with the staged row).
   cpu_baseline – the oracle's restatement of the reference's ListIntersectionKernel
             (bs_tc.cu:120-148) on the host cores, on a stride sample of source vertices.
   si      – summary of the batched set-intersection workload (1e6 pairs of sorted unique
@@ -227,15 +232,59 @@ def tc_config(n: int, m: int, m_input: int, max_out: int) -> dict:
     return dict(WORKLOAD, n=int(n), m=int(m), m_input=int(m_input), max_out_degree=int(max_out))
 
 
-def tc_kernel_bytes(off: np.ndarray) -> tuple[int, int]:
-    """(streamed suffix elements, algorithmic bytes per launch) of the batched count:
-    every oriented edge u->v streams the suffix of N+(u) after v, sum over u of
-    d+(u)(d+(u)-1)/2 elements of 4 B; each in-edge range is 8 B; each out-list is marked
-    once (4 B per oriented edge); two u64 offsets per vertex."""
-    d = np.diff(off.astype(np.int64))
-    elems = int((d * (d - 1) // 2).sum())
-    n, m = len(d), int(d.sum())
-    return elems, 4 * elems + 12 * m + 16 * n
+def tc_split(off: np.ndarray, adj: np.ndarray, K: int) -> dict:
+    """How the batched count of the oriented CSR (kept ids) splits its work when the top K
+    ranks form the dense core. Ranks order vertices by (degree, id), the orientation's own
+    order, so the counting form is this CSR relabelled by rank and c0 = n - K.
+
+    Streaming kernel: the in-edges u->v with u below the core and d+(v) >= 1 (heads without
+    out-edges get no work item); each streams the suffix of N+(u) after v (4 B per element)
+    and reads its range (8 B); every head with streamed in-edges marks its out-list once
+    (4 B per element); two u64 offsets per vertex. Core stage: the edges u->v of core rows
+    except the last of each row, each sweeping the 16-byte groups of N+(v)'s rank span up to
+    u's last group (kernel k_tc_core)."""
+    off = off.astype(np.int64)
+    n = len(off) - 1
+    dplus = np.diff(off)
+    m = int(off[-1])
+    src = np.repeat(np.arange(n, dtype=np.int64), dplus)
+    dst = adj[:m].astype(np.int64)
+    deg = dplus + np.bincount(dst, minlength=n)
+    rank = np.empty(n, np.int64)
+    rank[np.lexsort((np.arange(n), deg))] = np.arange(n)
+    # rows in rank order (the counting form's rows, still indexed by kept source ids)
+    dst = dst[np.lexsort((rank[dst], src))]
+    c0 = n - K
+    pos = np.arange(m, dtype=np.int64)
+    suffix = off[src + 1] - pos - 1
+    head_ok = dplus[dst] >= 1
+    streamed = (rank[src] < c0) & head_ok
+    sdeg = np.bincount(dst[streamed], minlength=n)
+    out = {"stream_elems": int(suffix[streamed].sum()), "stream_inedges": int(streamed.sum()),
+           "mark_elems": int(dplus[(sdeg >= 1) & (dplus >= 1)].sum())}
+    out["stream_bytes"] = (4 * out["stream_elems"] + 8 * out["stream_inedges"] +
+                           4 * out["mark_elems"] + 16 * n)
+    out["core_edges"] = int((rank[src] >= c0).sum())
+    rw = 4
+    while rw * 32 < K:
+        rw <<= 1
+    out["matrix_bytes"] = K * rw * 4 if K else 0
+    if K:
+        rdst = rank[dst]
+        # rank span of every out-list: its first and last element in rank order
+        nz = dplus > 0
+        lo = np.full(n, -1, np.int64)
+        hi = np.full(n, -1, np.int64)
+        lo[nz] = rdst[off[:-1][nz]]
+        hi[nz] = rdst[off[1:][nz] - 1]
+        sel = (rank[src] >= c0) & (pos != off[src + 1] - 1) & head_ok
+        u, v = src[sel], dst[sel]
+        g0 = ((lo[v] - c0) >> 5) >> 2
+        g1 = np.minimum(((hi[v] - c0) >> 5) >> 2, ((hi[u] - c0) >> 5) >> 2)
+        out["core_groups"] = int(np.where(g1 >= g0, g1 - g0 + 1, 0).sum())
+    else:
+        out["core_groups"] = 0
+    return out
 
 
 def cpu_baseline_tc(off: np.ndarray, adj: np.ndarray, target_s: float = 15.0) -> dict:
@@ -529,24 +578,26 @@ def serve_run(srv, gids, pools, reqs, rate: float | None, m_of: list[int]) -> di
 def measure_serve(args) -> dict:
     """Serving workload: saturation throughput from a burst of all requests, then Poisson
     arrivals at 0.5 / 0.8 / 0.95 of it; an HBM budget below the graphs' full footprint
-    (graphs + a quarter of all counting plans) forces plan eviction and admission waits."""
+    (graphs + a quarter of all counting plans, as the library sizes them: one count of every
+    graph on a server without a budget) forces plan eviction and admission waits."""
     import rtg
     graphs = serve_setup(SERVE_WORKLOAD["seed"])
     srv = rtg.Server(0)
     gids = [srv.add_graph(s, d) for _, s, d in graphs]
     infos = [srv.graph_info(x) for x in gids]
-    st0 = srv.stats()
-    srv.close()
-    plans = sum((i.m // 256 + i.n + 1) * 8 + (i.n + 1) * 12 + 4096 for i in infos)
-    budget = st0["resident_bytes"] + st0["buffer_bytes"] + plans // 4
-    srv = rtg.Server(0, budget_bytes=budget)
-    gids = [srv.add_graph(s, d) for _, s, d in graphs]
     rng = np.random.default_rng(SERVE_WORKLOAD["seed"])
     pools = []
     for i in infos:
         pools.append((rng.integers(0, i.n_sym, 250_000, dtype=np.uint32),
                       rng.integers(0, i.n_sym, 250_000, dtype=np.uint32)))
     m_of = [int(i.m) for i in infos]
+    serve_run(srv, gids, pools, [(g, 0, 0) for g in range(len(gids))], None, m_of)
+    st0 = srv.stats()
+    srv.close()
+    plans = st0["plan_bytes"]
+    budget = st0["resident_bytes"] + st0["buffer_bytes"] + plans // 4
+    srv = rtg.Server(0, budget_bytes=budget)
+    gids = [srv.add_graph(s, d) for _, s, d in graphs]
     nreq = SERVE_WORKLOAD["requests"]
     # warm-up: every graph's counting plan and both SI slots once
     warm = serve_requests(np.random.default_rng(1), len(gids), None, 200, pools)
@@ -663,7 +714,7 @@ def run_gpu(args, dist: Dist) -> None:
     want = g.tc(rtg.TC_BATCHED)[0]
     # ---- timed region: batched count, L2 flushed between steps
     launches0 = ctx.launches
-    ms_steps, kms_steps = [], []
+    ms_steps, kms_steps, core_steps = [], [], []
     dist.barrier()
     ctx.sync()
     with ClockSampler(dist.local) as clk:
@@ -674,7 +725,9 @@ def run_gpu(args, dist: Dist) -> None:
                 raise RuntimeError(f"count changed between steps: {total} != {want}")
             ms_steps.append(t.count_ms)
             kms_steps.append(t.main_kernel_ms)
+            core_steps.append(t.core_ms)
         ctx.sync()
+    core_ranks = int(t.core_ranks)
     dist.barrier()
     launches = ctx.launches - launches0  # kernels only: the L2 flush is a memset
     algo_bytes = t.algo_bytes
@@ -715,21 +768,30 @@ def run_gpu(args, dist: Dist) -> None:
             raise RuntimeError("end-to-end count differs")
     e2e_value, _ = aggregate(dist, m, sum(e2e_ms) / len(e2e_ms))
     kms = sum(kms_steps) / len(kms_steps)
+    core_ms = sum(core_steps) / len(core_steps)
     peaks = measured_peaks()
     off, adj = g.csr()
-    elems, kbytes = tc_kernel_bytes(off)
+    split = tc_split(off, adj, core_ranks)
+    elems, kbytes = split["stream_elems"], split["stream_bytes"]
     prof = profile_fields("tc_batched_rmat21")
     achieved = kbytes / (kms / 1e3) / 1e9
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",
                 "frac": achieved / peaks["hbm_gbs"], "traffic": profile_traffic("tc_batched_rmat21"),
                 "peak_source": peaks["source"], "kernel": "k_tc_warp", "kernel_ms": kms,
                 "algo_bytes_per_launch": kbytes, "streamed_elements": elems,
-                "algo_bytes_basis": "4 B per streamed suffix element + 8 B per in-edge range + "
-                                    "4 B per out-list element + 16 B of offsets per vertex",
+                "algo_bytes_basis": "4 B per streamed suffix element + 8 B per streamed in-edge "
+                                    "range + 4 B per out-list element marked + 16 B of offsets "
+                                    "per vertex (in-edges from sources below the dense core)",
                 "work_equiv_bytes": algo_bytes,
-                "work_equiv_gbs": algo_bytes / (kms / 1e3) / 1e9,
-                "work_equiv_basis": "4 x sum over oriented edges of (d+(u) + d+(v)) + 8 m: both "
-                                    "full out-lists per edge, which this kernel never streams"}
+                "work_equiv_gbs": algo_bytes / (ms_local / 1e3) / 1e9,
+                "work_equiv_basis": "4 x sum over oriented edges of (d+(u) + d+(v)) + 8 m over "
+                                    "the whole count's device time: both full out-lists per "
+                                    "edge, which the count never streams"}
+    core = {"ranks": core_ranks, "ms": core_ms, "edges": split["core_edges"],
+            "matrix_bytes": split["matrix_bytes"], "groups_swept": split["core_groups"],
+            "l2_gbs": (16 * split["core_groups"] / (core_ms / 1e3) / 1e9) if core_ms else None,
+            "kernels": "k_core_rows (matrix rows) + k_tc_core (word-AND count)",
+            "rule": "library choice: largest of 32768 .. 1024 top ranks with edge density >= 2.5 %"}
     if "issue_active" in prof:
         roofline["issue_active"] = prof["issue_active"]
     if "warp_instructions" in prof:
@@ -794,7 +856,7 @@ def run_gpu(args, dist: Dist) -> None:
                                      "no CUDA graph, default schedule, items built every call"},
                 "bucketed_over_plain": buck_value / plain_value,
                 "batched_over_bucketed": value / buck_value,
-                "roofline": roofline, "cpu_baseline": cpu, "clocks": clk.summary(),
+                "roofline": roofline, "core": core, "cpu_baseline": cpu, "clocks": clk.summary(),
                 "gpu_launches": int(launches), "schedule": tune, "si": si,
                 "serving": serving}
         print(json.dumps(line), flush=True)

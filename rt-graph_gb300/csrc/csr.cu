@@ -551,15 +551,17 @@ rtg_status in_edge_tail(rtg_ctx *ctx, CountCsr &cc, uint64_t *ek, uint64_t *othe
         return RTG_OK;
     }
     unsigned long long *w = ctx->d_scalars;
-    RTG_CUDA(ctx, cudaMemsetAsync(w, 0, 16, ctx->stream));
+    RTG_CUDA(ctx, cudaMemsetAsync(w, 0, 24, ctx->stream));
     k_stats<<<grid_for(ctx, n), kThreads, 0, ctx->stream>>>(cc.off, cc.adj, nullptr, mr, n, w,
                                                              (unsigned int *)(w + 1));
-    ctx->launches++;
+    enqueue_core_auto(ctx->stream, cc, w + 2);
+    ctx->launches += 2;
     RTG_CUDA(ctx, cudaGetLastError());
-    unsigned long long h[2];
-    RTG_CUDA(ctx, cudaMemcpyAsync(h, w, 16, cudaMemcpyDeviceToHost, ctx->stream));
+    unsigned long long h[3];
+    RTG_CUDA(ctx, cudaMemcpyAsync(h, w, 24, cudaMemcpyDeviceToHost, ctx->stream));
     RTG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
     cc.max_deg = (uint32_t)h[1];
+    cc.core_auto = (int64_t)h[2];
     cc.built = true;
     return RTG_OK;
 }
@@ -567,6 +569,7 @@ rtg_status in_edge_tail(rtg_ctx *ctx, CountCsr &cc, uint64_t *ek, uint64_t *othe
 rtg_status count_alloc(rtg_ctx *ctx, CountCsr &cc, uint32_t n, uint64_t m) {
     count_csr_free(cc);
     cc.n = n;
+    cc.core_auto = -1;
     RTG_TRY(dev_alloc(ctx, (void **)&cc.off, (n + 1ull) * 8));
     RTG_TRY(dev_alloc(ctx, (void **)&cc.in_off, (n + 1ull) * 8));
     RTG_TRY(dev_alloc(ctx, (void **)&cc.adj, m * 4 + kAdjPadBytes));

@@ -67,6 +67,7 @@ struct CountCsr {
     uint32_t n = 0;
     uint64_t m = 0;
     uint32_t max_deg = 0;
+    int64_t core_auto = -1;  // the library's dense-core size for this form (-1: not known)
     bool built = false;
 };
 
@@ -209,6 +210,9 @@ rtg_status tc_launch_async(rtg_ctx *ctx, rtg_graph *g, unsigned long long *h_tot
 // Device bytes the batched plan of g will hold (upper estimate; also the scratch that
 // tc_launch_direct needs).
 uint64_t tc_plan_estimate_bytes(const rtg_ctx *ctx, const rtg_graph *g);
+// the library's dense-core size of a counting form (its offsets complete on the stream)
+// into *out, a device word (tc.cu)
+void enqueue_core_auto(cudaStream_t st, const CountCsr &cc, unsigned long long *out);
 // The same count without a plan: the kernels are launched directly on ctx's stream with
 // their buffers carved from the caller's device scratch, which must stay untouched until
 // the count has completed.

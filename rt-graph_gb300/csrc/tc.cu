@@ -205,33 +205,45 @@ __host__ __device__ constexpr uint32_t core_row_words(uint32_t K) {
     return K ? w : 0u;
 }
 
-// largest core the schedule can pick on a graph of n vertices (sizes the core buffers)
-uint32_t core_max_ranks(uint32_t forced, uint32_t n) {
+// The library's choice: the largest candidate whose m - off[n - K] core edges reach the
+// density bar, 0 if none does.
+__device__ uint32_t auto_core(const uint64_t *__restrict__ off, uint32_t n, uint64_t m) {
+    for (int i = 0; i < kCoreCandidates; ++i) {
+        const uint32_t c = core_candidate(i);
+        if (c > n) continue;
+        const uint64_t ce = m - off[n - c];
+        if (1000ull * ce >= (uint64_t)kCoreMinDensityPerMille * c * (c - 1) / 2) return c;
+    }
+    return 0;
+}
+
+__global__ void k_core_auto(const uint64_t *__restrict__ off, uint32_t n, uint64_t m,
+                            unsigned long long *out) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) *out = auto_core(off, n, m);
+}
+
+// The core size a schedule gives a counting form: RTG_TC_CORE_NONE -> 0, a forced size ->
+// min(size, n), the library's choice -> the size cached when the form was built, or, for a
+// form built without it (one-shot counts, cache files), the largest candidate that fits
+// (the buffers' bound; the device picks the actual size).
+uint32_t core_max_ranks(uint32_t forced, const CountCsr &c) {
     if (forced == RTG_TC_CORE_NONE) return 0;
-    if (forced) return std::min(forced, n);
+    if (forced) return std::min(forced, c.n);
+    if (c.core_auto >= 0) return (uint32_t)c.core_auto;
     for (int i = 0; i < kCoreCandidates; ++i)
-        if (core_candidate(i) <= n) return core_candidate(i);
+        if (core_candidate(i) <= c.n) return core_candidate(i);
     return 0;
 }
 
 // The core of this count: `forced` ranks (RTG_TC_CORE_NONE: none), or with forced == 0 the
-// largest candidate whose m - off[n - K] core edges reach the density bar.
+// library's choice.
 __global__ void k_core_pick(const uint64_t *__restrict__ off, uint32_t n, uint64_t m,
                             uint32_t forced, unsigned long long *acc) {
     if (blockIdx.x || threadIdx.x) return;
     uint32_t K = 0;
     if (forced == RTG_TC_CORE_NONE) K = 0;
     else if (forced) K = min(forced, n);
-    else
-        for (int i = 0; i < kCoreCandidates; ++i) {
-            const uint32_t c = core_candidate(i);
-            if (c > n) continue;
-            const uint64_t ce = m - off[n - c];
-            if (1000ull * ce >= (uint64_t)kCoreMinDensityPerMille * c * (c - 1) / 2) {
-                K = c;
-                break;
-            }
-        }
+    else K = auto_core(off, n, m);
     acc[kAccCoreK] = K;
     acc[kAccCoreC0] = n - K;
     acc[kAccCoreRw] = core_row_words(K);
@@ -953,8 +965,11 @@ rtg_status batched_shape(rtg_ctx *ctx, const CountCsr &c, const rtg_config &cfg,
     bs->grid = ctx->sm_count * per_sm;
     bs->g1 = (int)std::max<uint64_t>(1, std::min<uint64_t>((c.n + 256ull) / 256,
                                                           ctx->sm_count * 16ull));
-    bs->core_forced = cfg.tc_core_ranks;
-    return core_shape(ctx, core_max_ranks(cfg.tc_core_ranks, c.n), bs);
+    const uint32_t K = core_max_ranks(cfg.tc_core_ranks, c);
+    // what the device pick is told: a size known on the host is passed as is
+    bs->core_forced = !K ? RTG_TC_CORE_NONE
+                         : (cfg.tc_core_ranks || c.core_auto >= 0 ? K : 0u);
+    return core_shape(ctx, K, bs);
 }
 
 // Device buffers of one batched count (a plan's, or carved from caller scratch).
@@ -973,8 +988,7 @@ void enqueue_items(cudaStream_t st, const CountCsr &c, const BatchedShape &bs, c
     uint32_t *vbase = b.vcnt + (c.n + 1ull);
     size_t cub_bytes = bs.cub_bytes;
     cudaMemsetAsync(b.acc, 0, kAccWords * sizeof(unsigned long long), st);
-    k_core_pick<<<1, 32, 0, st>>>(c.off, c.n, c.m, bs.core_max ? bs.core_forced : RTG_TC_CORE_NONE,
-                                  b.acc);
+    k_core_pick<<<1, 32, 0, st>>>(c.off, c.n, c.m, bs.core_forced, b.acc);
     k_item_counts<<<bs.g1, 256, 0, st>>>(c.off, c.in_off, c.in_rng, c.n, bs.pc.E, b.acc, b.vcnt,
                                          b.sdeg);
     cub::DeviceScan::ExclusiveSum(b.cub_tmp, cub_bytes, b.vcnt, vbase, (int64_t)c.n + 1, st);
@@ -1323,10 +1337,14 @@ rtg_status count_bucketed(rtg_ctx *ctx, rtg_graph *g, uint64_t *total, rtg_timin
 
 }  // namespace
 
+void enqueue_core_auto(cudaStream_t st, const CountCsr &cc, unsigned long long *out) {
+    k_core_auto<<<1, 32, 0, st>>>(cc.off, cc.n, cc.m, out);
+}
+
 uint64_t tc_plan_estimate_bytes(const rtg_ctx *ctx, const rtg_graph *g) {
     const CountCsr &c = g->cnt;
     const rtg_config cfg = effective_config(ctx, c.m);
-    const uint32_t K = core_max_ranks(cfg.tc_core_ranks, c.n);
+    const uint32_t K = core_max_ranks(cfg.tc_core_ranks, c);
     // items + vertex counts and their scan + sdeg + scan temporary (bounded by one word per
     // vertex) + totals and alignment + core matrix and spans
     return (c.m / cfg.tc_item_edges + c.n + 1) * 8 + (c.n + 1ull) * 8 + (c.n + 1ull) * 4 +

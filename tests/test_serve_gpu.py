@@ -153,12 +153,19 @@ def test_large_request_split_across_launches(graphs):
 
 
 def test_budget_admission_and_plan_eviction(graphs):
+    # the counting plans as the library sizes them: one count of each graph without a budget
     with rtg.Server(0) as srv:
         gids = add_all(srv, graphs[:3])
         st = srv.stats()
-        infos = [srv.graph_info(x) for x in gids]
+        sizes, before = [], st["plan_bytes"]
+        for gid in gids:
+            assert srv.poll(srv.submit_tc(gid))["status"] == rtg.OK
+            after = srv.stats()["plan_bytes"]
+            sizes.append(after - before)
+            before = after
     base = st["resident_bytes"] + st["buffer_bytes"]
-    plan = max((i.m // 256 + i.n + 1) * 8 + (i.n + 1) * 12 + 4096 for i in infos)
+    plan = max(sizes)
+    assert min(sizes) > 0
     # room for the three graphs and one counting plan, not two
     with rtg.Server(0, budget_bytes=base + plan + plan // 2) as srv:
         gids = add_all(srv, graphs[:3])
