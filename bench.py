@@ -759,11 +759,12 @@ def run_gpu(args, dist: Dist) -> None:
     hs[:] = s
     hd[:] = d
     ctx.tc_count_host_edges(hs, hd, rtg.ORIENT_DEGREE, rtg.TC_BATCHED)  # warm
-    e2e_ms = []
+    e2e_ms, e2e_stages = [], []
     for _ in range(max(1, min(args.steps, 5))):
         t0 = time.perf_counter()
         tot, te = ctx.tc_count_host_edges(hs, hd, rtg.ORIENT_DEGREE, rtg.TC_BATCHED)
         e2e_ms.append((time.perf_counter() - t0) * 1e3)
+        e2e_stages.append((te.h2d_ms, te.build_ms, te.count_ms))
         if tot != want:
             raise RuntimeError("end-to-end count differs")
     e2e_value, _ = aggregate(dist, m, sum(e2e_ms) / len(e2e_ms))
@@ -844,6 +845,10 @@ def run_gpu(args, dist: Dist) -> None:
                 "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(te.h2d_bytes),
                         "d2h_bytes_per_step": int(te.d2h_bytes),
                         "ms_per_step": sum(e2e_ms) / len(e2e_ms),
+                        "stages_ms": {k: statistics.median(x[i] for x in e2e_stages)
+                                      for i, k in enumerate(("h2d", "build", "count"))},
+                        "stages_basis": "device time per stage (CUDA events): edge pull over "
+                                        "the host link, counting-form build, batched count",
                         "api": "rtg_tc_count_host_edges (pinned host edges, CSR build included)"},
                 "plain": {"value": plain_value, "unit": UNIT,
                           "ms_per_step": sum(plain_ms) / len(plain_ms)},

@@ -60,3 +60,67 @@ def test_no_nvidia_smi(tmp_path, monkeypatch):
     with bench.ClockSampler(0) as clk:
         pass
     assert clk.summary() == {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+
+
+def _brute_split(off, adj, K):
+    """The batched count's work split restated element by element on a small graph: rank
+    vertices by (degree, id), take each out-list in rank order, stream the suffix after v of
+    every in-edge u->v from a source below the core (heads with out-edges only), and sweep,
+    for every core edge but the last of its row, the 16-byte groups of N+(v)'s rank span up
+    to u's last group."""
+    import numpy as np
+    n = len(off) - 1
+    rows = [list(adj[off[u]:off[u + 1]]) for u in range(n)]
+    deg = [len(rows[u]) for u in range(n)]
+    for u in range(n):
+        for v in rows[u]:
+            deg[v] += 1
+    order = sorted(range(n), key=lambda x: (deg[x], x))
+    rank = {x: r for r, x in enumerate(order)}
+    c0 = n - K
+    rrows = [sorted(rank[w] for w in rows[u]) for u in range(n)]
+    byrank = [None] * n
+    for u in range(n):
+        byrank[rank[u]] = rrows[u]
+    elems = inedges = 0
+    sdeg = [0] * n
+    for ru in range(c0):
+        r = byrank[ru]
+        for i, rv in enumerate(r):
+            if byrank[rv]:
+                elems += len(r) - i - 1
+                inedges += 1
+                sdeg[rv] += 1
+    mark = sum(len(byrank[rv]) for rv in range(n) if sdeg[rv] and byrank[rv])
+    groups = 0
+    for ru in range(c0, n):
+        r = byrank[ru]
+        for rv in r[:-1]:
+            if not byrank[rv]:
+                continue
+            g0 = ((byrank[rv][0] - c0) >> 5) >> 2
+            g1 = min(((byrank[rv][-1] - c0) >> 5) >> 2, ((r[-1] - c0) >> 5) >> 2)
+            groups += max(0, g1 - g0 + 1)
+    core_edges = sum(len(byrank[ru]) for ru in range(c0, n))
+    return elems, inedges, mark, groups, core_edges
+
+
+@pytest.mark.parametrize("K", [0, 1, 40, 200, 1000])
+def test_tc_split_matches_element_count(K):
+    """bench.tc_split (the roofline's algorithmic bytes of the streaming kernel and the core
+    stage's swept groups) against the element-by-element restatement."""
+    import numpy as np
+    import oracle
+    bench = _bench()
+    s, d = oracle.gen_rmat(10, 8, 0.57, 0.19, 0.19, seed=3)
+    off, adj = oracle.degree_csr(s, d)
+    K = min(K, len(off) - 1)
+    got = bench.tc_split(off, adj, K)
+    elems, inedges, mark, groups, core_edges = _brute_split(off, adj, K)
+    assert got["stream_elems"] == elems
+    assert got["stream_inedges"] == inedges
+    assert got["mark_elems"] == mark
+    assert got["core_groups"] == groups
+    assert got["core_edges"] == core_edges
+    n = len(off) - 1
+    assert got["stream_bytes"] == 4 * elems + 8 * inedges + 4 * mark + 16 * n
