@@ -68,8 +68,8 @@ __global__ void k_check_rows(const uint64_t *__restrict__ off, const uint32_t *_
 __global__ void k_check_ranges(const uint64_t *__restrict__ off, const uint32_t *__restrict__ adj,
                                const uint64_t *__restrict__ in_off,
                                const uint2 *__restrict__ in_rng, uint32_t n, uint64_t m,
-                               uint32_t *status) {
-    for (uint64_t e = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; e < m;
+                               uint64_t m_in, uint32_t *status) {
+    for (uint64_t e = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; e < m_in;
          e += (uint64_t)gridDim.x * blockDim.x) {
         const uint2 r = in_rng[e];
         const uint32_t v = row_of(in_off, n, e);
@@ -116,14 +116,16 @@ rtg_status check_csr(rtg_ctx *ctx, const Csr &c, bool above_vertex) {
 rtg_status check_count_form(rtg_ctx *ctx, const CountCsr &cc) {
     if (!cc.built) return RTG_OK;
     RTG_TRY(check_rows_of(ctx, cc.off, cc.adj, cc.n, cc.m, true));
-    k_check_offsets<<<grid_for(ctx, cc.n + 1ull), 256, 0, ctx->stream>>>(cc.in_off, cc.n, cc.m,
+    // in-edge offsets end at the in-edges held (a one-shot form holds those below its core)
+    const uint64_t mi = cc.inedges();
+    k_check_offsets<<<grid_for(ctx, cc.n + 1ull), 256, 0, ctx->stream>>>(cc.in_off, cc.n, mi,
                                                                          ctx->d_status);
     RTG_CUDA(ctx, cudaGetLastError());
     ctx->launches++;
     RTG_TRY(check_status_word(ctx));
-    if (cc.m) {
-        k_check_ranges<<<grid_for(ctx, cc.m), 256, 0, ctx->stream>>>(
-            cc.off, cc.adj, cc.in_off, cc.in_rng, cc.n, cc.m, ctx->d_status);
+    if (mi) {
+        k_check_ranges<<<grid_for(ctx, mi), 256, 0, ctx->stream>>>(
+            cc.off, cc.adj, cc.in_off, cc.in_rng, cc.n, cc.m, mi, ctx->d_status);
         RTG_CUDA(ctx, cudaGetLastError());
         ctx->launches++;
         RTG_TRY(check_status_word(ctx));

@@ -132,6 +132,8 @@ extern "C" rtg_status rtg_graph_save(rtg_ctx *ctx, const rtg_graph *g, const cha
         }
     };
     if (parts & kPartOri) csr(g->ori, true);
+    // a form holding part of its in-edges (a one-shot count's) is never written
+    if (st == RTG_OK && (parts & kPartCnt) && g->cnt.inedges() != g->cnt.m) st = RTG_ERR_STATE;
     if (st == RTG_OK && (parts & kPartCnt)) {
         const CountCsr &c = g->cnt;
         w.val(c.n);

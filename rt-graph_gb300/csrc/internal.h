@@ -68,7 +68,12 @@ struct CountCsr {
     uint64_t m = 0;
     uint32_t max_deg = 0;
     int64_t core_auto = -1;  // the library's dense-core size for this form (-1: not known)
+    // in-edges held: all m (kAllInEdges), or, in a one-shot count's form, only those of the
+    // rows below its dense core (the core count never reads the others)
+    uint64_t m_in = kAllInEdges;
     bool built = false;
+    static constexpr uint64_t kAllInEdges = ~0ull;
+    uint64_t inedges() const { return m_in == kAllInEdges ? m : m_in; }
 };
 
 struct TcPlan;   // cached per-graph counting plans (tc.cu)
@@ -213,6 +218,10 @@ uint64_t tc_plan_estimate_bytes(const rtg_ctx *ctx, const rtg_graph *g);
 // the library's dense-core size of a counting form (its offsets complete on the stream)
 // into *out, a device word (tc.cu)
 void enqueue_core_auto(cudaStream_t st, const CountCsr &cc, unsigned long long *out);
+// the dense-core size a schedule setting (rtg_config.tc_core_ranks) gives a counting form and
+// the first adj index of its core rows, into out[0] and out[1] (tc.cu)
+void enqueue_core_choice(cudaStream_t st, const CountCsr &cc, uint32_t setting,
+                         unsigned long long *out);
 // The same count without a plan: the kernels are launched directly on ctx's stream with
 // their buffers carved from the caller's device scratch, which must stay untouched until
 // the count has completed.

@@ -222,6 +222,17 @@ __global__ void k_core_auto(const uint64_t *__restrict__ off, uint32_t n, uint64
     if (blockIdx.x == 0 && threadIdx.x == 0) *out = auto_core(off, n, m);
 }
 
+// out[0] = the core size of a schedule setting (as k_core_pick), out[1] = off[n - size]
+__global__ void k_core_choice(const uint64_t *__restrict__ off, uint32_t n, uint64_t m,
+                              uint32_t setting, unsigned long long *out) {
+    if (blockIdx.x || threadIdx.x) return;
+    const uint32_t K = setting == RTG_TC_CORE_NONE ? 0u
+                       : setting                   ? min(setting, n)
+                                                   : auto_core(off, n, m);
+    out[0] = K;
+    out[1] = off[n - K];
+}
+
 // The core size a schedule gives a counting form: RTG_TC_CORE_NONE -> 0, a forced size ->
 // min(size, n), the library's choice -> the size cached when the form was built, or, for a
 // form built without it (one-shot counts, cache files), the largest candidate that fits
@@ -1339,6 +1350,11 @@ rtg_status count_bucketed(rtg_ctx *ctx, rtg_graph *g, uint64_t *total, rtg_timin
 
 void enqueue_core_auto(cudaStream_t st, const CountCsr &cc, unsigned long long *out) {
     k_core_auto<<<1, 32, 0, st>>>(cc.off, cc.n, cc.m, out);
+}
+
+void enqueue_core_choice(cudaStream_t st, const CountCsr &cc, uint32_t setting,
+                         unsigned long long *out) {
+    k_core_choice<<<1, 32, 0, st>>>(cc.off, cc.n, cc.m, setting, out);
 }
 
 uint64_t tc_plan_estimate_bytes(const rtg_ctx *ctx, const rtg_graph *g) {
