@@ -28,14 +28,17 @@ uint32_t lg(uint64_t x) {
     return r;
 }
 
-std::string device_key(const rtg_ctx *ctx) {
-    char b[64];
-    snprintf(b, sizeof b, "sm%d/cc%d.%d", ctx->sm_count, ctx->cc_major, ctx->cc_minor);
-    return b;
-}
-
 const uint32_t *cfg_words(const rtg_config &c) { return reinterpret_cast<const uint32_t *>(&c); }
 constexpr int kCfgWords = sizeof(rtg_config) / sizeof(uint32_t);
+
+// the device, and the schedule's word count: entries written for another rtg_config layout
+// do not match
+std::string device_key(const rtg_ctx *ctx) {
+    char b[64];
+    snprintf(b, sizeof b, "sm%d/cc%d.%d/w%d", ctx->sm_count, ctx->cc_major, ctx->cc_minor,
+             kCfgWords);
+    return b;
+}
 
 bool cache_lookup(const char *path, const std::string &key, rtg_config *cfg, double *ms) {
     if (!path) return false;
@@ -110,11 +113,13 @@ extern "C" rtg_status rtg_tune_tc(rtg_ctx *ctx, rtg_graph *g, const char *cache_
         res->from_cache = 1;
         return RTG_OK;
     }
-    auto run = [&](const rtg_config &c, uint64_t *total, double *ms) -> rtg_status {
+    auto run = [&](const rtg_config &c, uint64_t *total, double *ms,
+                   uint32_t *core = nullptr) -> rtg_status {
         rtg_status st = rtg_set_config(ctx, &c);
         if (st != RTG_OK) return st;
         rtg_timing t{};
         RTG_TRY(tc_count(ctx, g, RTG_TC_BATCHED, total, &t));  // builds the plan
+        if (core) *core = t.core_ranks;
         std::vector<double> v;
         for (int r = 0; r < kReps; ++r) {
             RTG_TRY(rtg_flush_l2(ctx));
@@ -132,7 +137,8 @@ extern "C" rtg_status rtg_tune_tc(rtg_ctx *ctx, rtg_graph *g, const char *cache_
     def.tc_core_ranks = 0;
     uint64_t want = 0;
     double def_ms = 0;
-    rtg_status st = run(def, &want, &def_ms);
+    uint32_t core0 = 0;  // the library's dense-core size on this graph
+    rtg_status st = run(def, &want, &def_ms, &core0);
     if (st != RTG_OK) {
         ctx->cfg = saved;
         return st;
@@ -159,6 +165,34 @@ extern "C" rtg_status rtg_tune_tc(rtg_ctx *ctx, rtg_graph *g, const char *cache_
                     best = c;
                 }
             }
+    // the dense core on the best schedule: none, half and twice the library's choice (within
+    // 1024 .. 32768 ranks), or, where it chose none, 4096 and 16384 ranks
+    std::vector<uint32_t> cores;
+    if (core0) {
+        cores.push_back(RTG_TC_CORE_NONE);
+        if (core0 / 2 >= 1024) cores.push_back(core0 / 2);
+        if (core0 < RTG_TC_CORE_MAX_RANKS)
+            cores.push_back(std::min<uint32_t>(2 * core0, RTG_TC_CORE_MAX_RANKS));
+    } else {
+        for (uint32_t K : {4096u, 16384u})
+            if (K <= g->cnt.n) cores.push_back(K);
+    }
+    const rtg_config sched = best;
+    for (uint32_t K : cores) {
+        rtg_config c = sched;
+        c.tc_core_ranks = K;
+        uint64_t got = 0;
+        double ms = 0;
+        res->candidates++;
+        if (run(c, &got, &ms) != RTG_OK || got != want) {
+            res->rejected++;
+            continue;
+        }
+        if (ms < best_ms) {
+            best_ms = ms;
+            best = c;
+        }
+    }
     ctx->last_error.clear();
     rtg_set_config(ctx, &best);
     res->best = best;

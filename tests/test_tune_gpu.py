@@ -19,7 +19,8 @@ def test_tune_tc_keeps_exact_count_and_caches(tmp_path):
     with rtg.Context(0) as ctx:
         g = ctx.graph_from_edges(s, d).build(rtg.ORIENT_DEGREE)
         r = g.tune(cache)
-        assert not r["from_cache"] and r["candidates"] == 36
+        # 36 schedules, then up to 3 dense-core sizes on the best of them
+        assert not r["from_cache"] and 37 <= r["candidates"] <= 39
         assert r["rejected"] < r["candidates"]
         assert r["best_ms"] <= r["default_ms"]
         assert ctx.config().as_dict()["tc_item_edges"] == r["best"]["tc_item_edges"]
