@@ -343,11 +343,23 @@ def _check_oriented_csr(off, adj):
 
 
 def test_config4_rmat21_full_size(ctx):
-    """R-MAT scale 21, ef 16: PLAIN == BATCHED == oracle merge count; CSR checked."""
+    """R-MAT scale 21, ef 16: PLAIN == BATCHED == oracle merge count; CSR checked; the
+    batched and one-shot counts also without a dense core and with cores of 4096 and 32768
+    top ranks (the library picks 24576 here)."""
     s, d = rtg.gen_rmat(21, 16, 0.57, 0.19, 0.19, seed=42)
     g = ctx.graph_from_edges(s, d).build(rtg.ORIENT_DEGREE)
     off, adj = g.csr()
     _check_oriented_csr(off, adj)
     want = oracle.tc_merge(off, adj)
-    assert g.tc(rtg.TC_BATCHED)[0] == want
+    got, t = g.tc(rtg.TC_BATCHED)
+    assert (got, t.core_ranks) == (want, 24576)
     assert g.tc(rtg.TC_PLAIN)[0] == want
+    saved = ctx.config().as_dict()
+    try:
+        for K in (rtg.TC_CORE_NONE, 4096, 32768):
+            ctx.set_config(**dict(saved, tc_core_ranks=K))
+            got, t = g.tc(rtg.TC_BATCHED)
+            assert (got, t.core_ranks) == (want, 0 if K == rtg.TC_CORE_NONE else K)
+            assert ctx.tc_count_host_edges(s, d, rtg.ORIENT_DEGREE, rtg.TC_BATCHED)[0] == want
+    finally:
+        ctx.set_config(**saved)
