@@ -315,6 +315,8 @@ rtg_status graph_load_cached(rtg_ctx *ctx, const char *path, rtg_graph **out) {
         if (st == RTG_OK) st = upload(ctx, &c.adj, hc.adj, hc.m, kAdjPadBytes);
         if (st == RTG_OK) st = upload(ctx, &c.in_off, hc.in_off, hc.n + 1ull, 0);
         if (st == RTG_OK) st = upload(ctx, &c.in_rng, hc.rng, hc.m, 0);
+        // the library's dense-core size, from the offsets already on the host
+        c.core_auto = hc.m ? core_auto_host(hc.off.data(), hc.n, hc.m) : 0;
         c.built = st == RTG_OK;
     }
     if (parts & kPartSym) up_csr(g->sym, hs);

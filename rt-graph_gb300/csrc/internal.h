@@ -218,6 +218,8 @@ uint64_t tc_plan_estimate_bytes(const rtg_ctx *ctx, const rtg_graph *g);
 // the library's dense-core size of a counting form (its offsets complete on the stream)
 // into *out, a device word (tc.cu)
 void enqueue_core_auto(cudaStream_t st, const CountCsr &cc, unsigned long long *out);
+// the same choice from host offsets (forms read from a cache file) (tc.cu)
+uint32_t core_auto_host(const uint64_t *off, uint32_t n, uint64_t m);
 // the dense-core size a schedule setting (rtg_config.tc_core_ranks) gives a counting form and
 // the first adj index of its core rows, into out[0] and out[1] (tc.cu)
 void enqueue_core_choice(cudaStream_t st, const CountCsr &cc, uint32_t setting,

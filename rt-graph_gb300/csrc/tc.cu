@@ -206,8 +206,8 @@ __host__ __device__ constexpr uint32_t core_row_words(uint32_t K) {
 }
 
 // The library's choice: the largest candidate whose m - off[n - K] core edges reach the
-// density bar, 0 if none does.
-__device__ uint32_t auto_core(const uint64_t *__restrict__ off, uint32_t n, uint64_t m) {
+// density bar, 0 if none does (on the device, and on the host for forms read from a file).
+__host__ __device__ uint32_t auto_core(const uint64_t *__restrict__ off, uint32_t n, uint64_t m) {
     for (int i = 0; i < kCoreCandidates; ++i) {
         const uint32_t c = core_candidate(i);
         if (c > n) continue;
@@ -1347,6 +1347,8 @@ rtg_status count_bucketed(rtg_ctx *ctx, rtg_graph *g, uint64_t *total, rtg_timin
 }
 
 }  // namespace
+
+uint32_t core_auto_host(const uint64_t *off, uint32_t n, uint64_t m) { return auto_core(off, n, m); }
 
 void enqueue_core_auto(cudaStream_t st, const CountCsr &cc, unsigned long long *out) {
     k_core_auto<<<1, 32, 0, st>>>(cc.off, cc.n, cc.m, out);
