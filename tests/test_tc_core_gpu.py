@@ -138,3 +138,22 @@ def test_plan_follows_core_setting(ctx):
                 seen.append(t.core_ranks)
     assert seen == [512] * 3 + [0] * 3 + [2048] * 3 + [512] * 3
     g.close()
+
+
+def test_loaded_graph_keeps_the_core(ctx, tmp_path):
+    """A graph read back from its cache file picks the same core (from the file's offsets)
+    and counts the same, resident and with a forced core."""
+    s, d = rtg.gen_rmat(16, 16, 0.57, 0.19, 0.19, seed=8)
+    g = ctx.graph_from_edges(s, d).build(rtg.ORIENT_DEGREE)
+    want, t = g.tc(rtg.TC_BATCHED)
+    assert t.core_ranks > 0
+    path = tmp_path / "g.rtgcsr"
+    g.save(str(path))
+    h = ctx.graph_load(str(path), rtg.FMT_RTG_CSR)
+    got, t2 = h.tc(rtg.TC_BATCHED)
+    assert (got, t2.core_ranks) == (want, t.core_ranks)
+    with core_config(ctx, tc_core_ranks=3000):
+        assert h.tc(rtg.TC_BATCHED)[0] == want
+        assert h.tc(rtg.TC_BUCKETED)[0] == want
+    h.close()
+    g.close()
