@@ -636,6 +636,54 @@ __global__ void k_edge_pull(const uint4 *__restrict__ hs, const uint4 *__restric
     }
 }
 
+// The one-shot batched count of edges already in tg.d_src / tg.d_dst (context scratch; the
+// host -> device stage was bracketed by ev[6] and now ends): the counting form is built
+// straight from them (no oriented CSR) and counted with direct launches (no plan). Fills the
+// stage times of t. tg only borrows scratch: nothing in it is freed.
+static rtg_status one_shot_count(rtg_ctx *ctx, rtg_graph &tg, const EdgePrePass *pre,
+                                 uint64_t h2d_bytes, uint64_t *out_total, rtg_timing &t) {
+    rtg_graph *g = &tg;
+    RTG_CUDA(ctx, cudaEventRecord(ctx->ev[7], ctx->stream));
+    rtg_status s;
+    {
+        NvtxRange r("one-shot counting-form build");
+        s = build_count_direct(ctx, g, true, true, pre);
+    }
+    void *scr = nullptr;
+    const uint64_t need = s == RTG_OK ? tc_plan_estimate_bytes(ctx, g) : 0;
+    if (s == RTG_OK) s = scratch(ctx, 6, need, &scr);
+    unsigned long long h = 0;
+    if (s == RTG_OK) {
+        float h2d = 0;
+        cudaEventElapsedTime(&h2d, ctx->ev[6], ctx->ev[7]);
+        t.h2d_ms = h2d;
+        t.h2d_bytes = h2d_bytes;
+        t.algo_bytes = 0;
+        cudaError_t e = cudaEventRecord(ctx->ev[0], ctx->stream);
+        if (e != cudaSuccess) s = cuda_fail(ctx, e, "event", __FILE__, __LINE__);
+    }
+    if (s == RTG_OK) {
+        NvtxRange r("one-shot batched count");
+        s = tc_launch_direct(ctx, g, scr, need, &h);
+    }
+    if (s == RTG_OK) {
+        cudaError_t e = cudaEventRecord(ctx->ev[1], ctx->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+        if (e != cudaSuccess) s = cuda_fail(ctx, e, "count", __FILE__, __LINE__);
+    }
+    if (s == RTG_OK) s = check_status_word(ctx);
+    tg.d_src = tg.d_dst = nullptr;
+    tg.cnt = CountCsr{};
+    if (s != RTG_OK) return s;
+    float ms = 0, bms = 0;
+    cudaEventElapsedTime(&ms, ctx->ev[0], ctx->ev[1]);
+    cudaEventElapsedTime(&bms, ctx->ev[7], ctx->ev[0]);  // device time of the build
+    t.count_ms = t.main_kernel_ms = ms;
+    t.build_ms = bms;
+    *out_total = h;
+    return RTG_OK;
+}
+
 rtg_status rtg_tc_count_host_edges(rtg_ctx *ctx, const uint32_t *src, const uint32_t *dst,
                                    uint64_t m, rtg_orient orient, rtg_tc_mode mode,
                                    uint64_t *out_total, rtg_timing *timing) {
@@ -694,44 +742,7 @@ rtg_status rtg_tc_count_host_edges(rtg_ctx *ctx, const uint32_t *src, const uint
             RTG_CUDA(ctx, cudaMemcpyAsync(tg.d_src, src, m * 4, cudaMemcpyHostToDevice, ctx->stream));
             RTG_CUDA(ctx, cudaMemcpyAsync(tg.d_dst, dst, m * 4, cudaMemcpyHostToDevice, ctx->stream));
         }
-        RTG_CUDA(ctx, cudaEventRecord(ctx->ev[7], ctx->stream));
-        rtg_status s;
-        {
-            NvtxRange r("one-shot counting-form build");
-            s = build_count_direct(ctx, g, true, true, have_pre ? &pre : nullptr);
-        }
-        void *scr = nullptr;
-        const uint64_t need = s == RTG_OK ? tc_plan_estimate_bytes(ctx, g) : 0;
-        if (s == RTG_OK) s = scratch(ctx, 6, need, &scr);
-        unsigned long long h = 0;
-        if (s == RTG_OK) {
-            float h2d = 0;
-            cudaEventElapsedTime(&h2d, ctx->ev[6], ctx->ev[7]);
-            t.h2d_ms = h2d;
-            t.h2d_bytes = m * 8;
-            t.algo_bytes = 0;
-            cudaError_t e = cudaEventRecord(ctx->ev[0], ctx->stream);
-            if (e != cudaSuccess) s = cuda_fail(ctx, e, "event", __FILE__, __LINE__);
-        }
-        if (s == RTG_OK) {
-            NvtxRange r("one-shot batched count");
-            s = tc_launch_direct(ctx, g, scr, need, &h);
-        }
-        if (s == RTG_OK) {
-            cudaError_t e = cudaEventRecord(ctx->ev[1], ctx->stream);
-            if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
-            if (e != cudaSuccess) s = cuda_fail(ctx, e, "count", __FILE__, __LINE__);
-        }
-        if (s == RTG_OK) s = check_status_word(ctx);
-        tg.d_src = tg.d_dst = nullptr;  // borrowed scratch: nothing here is freed
-        tg.cnt = CountCsr{};
-        if (s != RTG_OK) return s;
-        float ms = 0, bms = 0;
-        cudaEventElapsedTime(&ms, ctx->ev[0], ctx->ev[1]);
-        cudaEventElapsedTime(&bms, ctx->ev[7], ctx->ev[0]);  // device time of the build
-        t.count_ms = t.main_kernel_ms = ms;
-        t.build_ms = bms;
-        *out_total = h;
+        RTG_TRY(one_shot_count(ctx, tg, have_pre ? &pre : nullptr, m * 8, out_total, t));
         t.d2h_bytes = 8;
         t.kernel_launches = ctx->launches - l0;
         t.total_ms = now_ms() - t0;
@@ -770,6 +781,48 @@ rtg_status rtg_tc_count_host_csr(rtg_ctx *ctx, const int32_t *offsets, const int
     rtg_timing t{};
     double t0 = now_ms();
     uint64_t l0 = ctx->launches;
+    if (mode == RTG_TC_BATCHED) {
+        // one-shot: the CSR's edges are counted like a host edge list (the counting form built
+        // straight from them, direct launches), after the same validation as a graph handle's
+        if (!offsets || nodes < 0 || edges < 0 || (edges && !adjs)) return RTG_ERR_INVALID_ARG;
+        if (offsets[nodes] != edges || offsets[0] != 0)
+            return fail(ctx, RTG_ERR_INVALID_ARG,
+                        "offsets[0] must be 0 and offsets[nodes] == edges");
+        const uint64_t n = (uint64_t)nodes, m = (uint64_t)edges;
+        const uint64_t mpad = (m + 63) & ~63ull, npad = (n + 1 + 63) & ~63ull;
+        rtg_graph tg;
+        void *pe = nullptr, *pc = nullptr;
+        RTG_CUDA(ctx, cudaEventRecord(ctx->ev[6], ctx->stream));
+        RTG_TRY(scratch(ctx, 2, mpad * 8 + 256, &pe));
+        tg.d_src = static_cast<uint32_t *>(pe);
+        tg.d_dst = tg.d_src + mpad;
+        tg.m_input = m;
+        // int32 offsets and ids in, u64 offsets as the validation kernel's by-product
+        RTG_TRY(scratch(ctx, 1, npad * 16 + mpad * 4 + 256, &pc));
+        int32_t *d_off32 = static_cast<int32_t *>(pc), *d_adj32 = d_off32 + npad;
+        uint64_t *d_off64 = reinterpret_cast<uint64_t *>(d_adj32 + mpad);
+        RTG_CUDA(ctx, cudaMemcpyAsync(d_off32, offsets, (n + 1) * 4, cudaMemcpyHostToDevice,
+                                      ctx->stream));
+        if (m)
+            RTG_CUDA(ctx, cudaMemcpyAsync(d_adj32, adjs, m * 4, cudaMemcpyHostToDevice,
+                                          ctx->stream));
+        const int grid = std::max(1, std::min(ctx->sm_count * 8, (int)((n + 256) / 256)));
+        k_csr_from_i32<<<grid, 256, 0, ctx->stream>>>(d_off32, d_adj32, (uint32_t)n, m, d_off64,
+                                                      tg.d_dst, tg.d_src, ctx->d_status);
+        ctx->launches++;
+        RTG_CUDA(ctx, cudaGetLastError());
+        if (check_status_word(ctx) != RTG_OK) {  // synchronises
+            tg.d_src = tg.d_dst = nullptr;
+            return fail(ctx, RTG_ERR_INVALID_ARG,
+                        "CSR rows must be sorted ascending with ids in [0, nodes)");
+        }
+        RTG_TRY(one_shot_count(ctx, tg, nullptr, (n + 1) * 4 + m * 4, out_total, t));
+        t.d2h_bytes = 8;
+        t.kernel_launches = ctx->launches - l0;
+        t.total_ms = now_ms() - t0;
+        if (timing) *timing = t;
+        return RTG_OK;
+    }
     rtg_graph *g = nullptr;
     RTG_TRY(rtg_graph_from_host_csr(ctx, offsets, adjs, nodes, edges, &g));
     t.h2d_ms = now_ms() - t0;

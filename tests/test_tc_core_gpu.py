@@ -53,6 +53,10 @@ def test_forced_core_sizes_agree(ctx, K):
                 assert (t.core_ms > 0) == (want_k > 0)
             got, _ = ctx.tc_count_host_edges(s, d, rtg.ORIENT_DEGREE, rtg.TC_BATCHED)
             assert got == rec["triangles"], (name, K, "one-shot")
+            off, adj = g.csr()
+            got, _ = ctx.tc_count_host_csr(off.astype(np.int32), adj.astype(np.int32),
+                                           rtg.TC_BATCHED)
+            assert got == rec["triangles"], (name, K, "host CSR")
         g.close()
 
 

@@ -147,6 +147,36 @@ def test_drop_in_host_csr_and_host_edges(ctx):
 
 
 @pytest.mark.parametrize("name", sorted(TC))
+def test_host_csr_batched_all_golden(ctx, name):
+    """rtg_tc_count_host_csr (the reference's CountOnGPU entry) in the batched form counts
+    the CSR's edges like a one-shot edge list; the golden count on every golden graph."""
+    rec = TC[name]
+    s, d = golden_edges(rec)
+    pairs = np.stack([s.astype(np.int32), d.astype(np.int32)], axis=1)
+    _, _, off, adj = oracle.reference_csr(pairs)
+    got, t = ctx.tc_count_host_csr(off, adj, rtg.TC_BATCHED)
+    assert got == rec["triangles"]
+    assert t.h2d_bytes == 4 * (len(off) + len(adj))
+
+
+def test_host_csr_batched_refuses_bad_csrs(ctx):
+    off = np.array([0, 2, 3, 3], np.int32)
+    for adj in (np.array([2, 1, 2], np.int32),      # row 0 not ascending
+                np.array([1, 3, 2], np.int32),      # id past the vertices
+                np.array([1, -1, 2], np.int32)):    # negative id
+        with pytest.raises(rtg.RtgError) as e:
+            ctx.tc_count_host_csr(off, adj, rtg.TC_BATCHED)
+        assert e.value.status == rtg.ERR_INVALID_ARG
+    with pytest.raises(rtg.RtgError) as e:           # offsets not ending at the edges
+        ctx.tc_count_host_csr(np.array([0, 2, 3, 4], np.int32), np.array([1, 2, 2], np.int32),
+                              rtg.TC_BATCHED)
+    assert e.value.status == rtg.ERR_INVALID_ARG
+    # the context still counts afterwards
+    got, _ = ctx.tc_count_host_csr(off, np.array([1, 2, 2], np.int32), rtg.TC_BATCHED)
+    assert got == 1
+
+
+@pytest.mark.parametrize("name", sorted(TC))
 def test_one_shot_host_edges_all_golden(ctx, name):
     """rtg_tc_count_host_edges with the degree orientation: the batched form builds the
     counting form straight from the edges; both forms give the reference's count."""
