@@ -293,7 +293,11 @@ rtg_status rtg_tc_count_host_edges(rtg_ctx *ctx, const uint32_t *src, const uint
 rtg_status rtg_tc_list(rtg_ctx *ctx, rtg_graph *g, uint64_t *out_offsets, uint32_t *out_elems,
                        uint64_t out_capacity, rtg_timing *timing);
 /* Replaces CountOnGPU (tc/bs_tc/bs_tc.h:5): host int32 CSR in, count out (uint64
- * instead of the reference's uint32). */
+ * instead of the reference's uint32). Rows must be strictly ascending with ids in
+ * [0, nodes) (RTG_ERR_INVALID_ARG otherwise). PLAIN counts the CSR as given (an acyclic
+ * orientation with every edge once, as the reference's preprocessing writes it); BATCHED
+ * counts the CSR's edges as a one-shot edge list (counting form built from them, direct
+ * launches), BUCKETED through a graph handle. */
 rtg_status rtg_tc_count_host_csr(rtg_ctx *ctx, const int32_t *offsets, const int32_t *adjs,
                                  int32_t nodes, int64_t edges, rtg_tc_mode mode,
                                  uint64_t *out_total, rtg_timing *timing);
