@@ -60,6 +60,10 @@ def test_every_six_vertex_graph_total(ctx, six, orient, core):
             assert got == int(tri.sum()), mode
         got, _ = ctx.tc_count_host_edges(s, d, rtg.ORIENT_DEGREE, rtg.TC_BATCHED)
         assert got == int(tri.sum())
+        off, adj = g.csr()  # the host-CSR entry, batched: the CSR's edges as a one-shot list
+        got, _ = ctx.tc_count_host_csr(off.astype(np.int32), adj.astype(np.int32),
+                                       rtg.TC_BATCHED)
+        assert got == int(tri.sum())
     finally:
         ctx.set_config(**saved)
     g.close()
