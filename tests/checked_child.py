@@ -47,8 +47,14 @@ def parity() -> None:
             ctx.set_config(**saved)
             g.close()
         s, d = rtg.gen_rmat(14, 16, seed=2)
+        off, adj = oracle.degree_csr(s, d)
+        want = oracle.tc_merge(off, adj)
         got, _ = ctx.tc_count_host_edges(s, d, rtg.ORIENT_DEGREE, rtg.TC_BATCHED)
-        assert got == oracle.tc_merge(*oracle.degree_csr(s, d))
+        assert got == want
+        # the host-CSR entry's one-shot form (in-edges below the core only), checked
+        got, _ = ctx.tc_count_host_csr(off.astype(np.int32), adj.astype(np.int32),
+                                       rtg.TC_BATCHED)
+        assert got == want
         off, el, pa, pb, exp = rtg.gen_si_pairs(20_000, seed=9)
         sets = ctx.sets(off, el)
         saved = ctx.config().as_dict()
