@@ -443,6 +443,23 @@ def measure_si(args, dist: Dist, ctx, cpu: bool) -> dict:
         if not np.array_equal(hout, exp):
             raise RuntimeError("end-to-end SI counts differ")
     e2e_value, _ = aggregate(dist, np_, sum(e2e_ms) / len(e2e_ms))
+    # materialised intersections of the same pairs: count -> scan -> write, elements to the
+    # host; checked against the expected counts
+    moff, mel, _ = sets.materialize(pa, pb)  # sizes the output
+    mat_dev, mat_wall = [], []
+    for _ in range(3):
+        ctx.flush_l2()
+        t0 = time.perf_counter()
+        moff, mel, tm = sets.materialize(pa, pb, capacity=len(mel))
+        mat_wall.append((time.perf_counter() - t0) * 1e3)
+        mat_dev.append(tm.count_ms)
+    if not np.array_equal(np.diff(moff.astype(np.int64)), exp.astype(np.int64)):
+        raise RuntimeError("materialised intersections differ from the expected counts")
+    materialize = {"pairs_per_s": np_ / (statistics.median(mat_dev) / 1e3),
+                   "device_ms": statistics.median(mat_dev), "wall_ms": statistics.median(mat_wall),
+                   "elements_out": int(len(mel)), "d2h_bytes": int(tm.d2h_bytes),
+                   "api": "rtg_si_materialize (count -> scan -> write, offsets and elements "
+                          "copied to the host; device_ms excludes the copy)"}
     kms = sum(kms_steps) / len(kms_steps)
     peaks = measured_peaks()
     achieved = algo / (kms / 1e3) / 1e9
@@ -472,6 +489,7 @@ def measure_si(args, dist: Dist, ctx, cpu: bool) -> dict:
         "clocks": clk.summary(),
         "cpu_baseline": None,
         "schedule": tune,
+        "materialize": materialize,
     }
     if cpu and dist.rank == 0 and dist.ws == 1:
         res["cpu_baseline"] = cpu_baseline_si(off, el, pa, pb)
@@ -492,7 +510,7 @@ def run_gpu_si(args, dist: Dist) -> None:
                 "e2e": r["e2e"], "plain": r["plain"], "batched_over_plain": r["batched_over_plain"],
                 "roofline": r["roofline"], "cpu_baseline": r["cpu_baseline"],
                 "clocks": r["clocks"], "gpu_launches": r["launches"],
-                "schedule": r["schedule"]}
+                "schedule": r["schedule"], "materialize": r["materialize"]}
         print(json.dumps(line), flush=True)
     ctx.close()
 
@@ -801,6 +819,22 @@ def run_gpu(args, dist: Dist) -> None:
     roofline.update(dram_view(roofline["traffic"], kms, peaks["hbm_gbs"],
                               "most of the algorithmic bytes are served from L2; the limiter "
                               "is instruction issue (issue_active), not DRAM (dram_frac)"))
+    # per-edge triangle lists of the same graph (count -> scan -> write over the oriented
+    # CSR's edges, lists copied to the host): every triangle once
+    tl_dev, tl_wall = [], []
+    for _ in range(2):
+        t0 = time.perf_counter()
+        loff, lw, tl = g.tc_list()
+        tl_wall.append((time.perf_counter() - t0) * 1e3)
+        tl_dev.append(tl.count_ms)
+    if int(loff[-1]) != want:
+        raise RuntimeError("triangle lists do not hold every triangle once")
+    tc_list = {"triangles_per_s": want / (min(tl_dev) / 1e3), "device_ms": min(tl_dev),
+               "wall_ms": min(tl_wall), "elements_out": int(loff[-1]),
+               "d2h_bytes": int(tl.d2h_bytes),
+               "api": "rtg_tc_list (count -> scan -> write per oriented edge, offsets and "
+                      "third vertices copied to the host; device_ms excludes the copy)"}
+    del loff, lw
     cpu = None
     if dist.rank == 0 and dist.ws == 1 and not args.no_cpu_baseline:
         cpu = cpu_baseline_tc(off, adj)
@@ -816,7 +850,7 @@ def run_gpu(args, dist: Dist) -> None:
               "roofline": {k: r["roofline"][k] for k in ("achieved", "peak", "unit", "frac",
                                                          "traffic", "kernel", "dram_gbs",
                                                          "dram_frac") if k in r["roofline"]},
-              "gpu_launches": r["launches"],
+              "gpu_launches": r["launches"], "materialize": r["materialize"],
               "schedule": r["schedule"]["best"] if r["schedule"] else "library default"}
     serving = None
     if not args.tc_only and not args.no_serve and dist.rank == 0:
@@ -861,7 +895,8 @@ def run_gpu(args, dist: Dist) -> None:
                                      "no CUDA graph, default schedule, items built every call"},
                 "bucketed_over_plain": buck_value / plain_value,
                 "batched_over_bucketed": value / buck_value,
-                "roofline": roofline, "core": core, "cpu_baseline": cpu, "clocks": clk.summary(),
+                "roofline": roofline, "core": core, "tc_list": tc_list, "cpu_baseline": cpu,
+                "clocks": clk.summary(),
                 "gpu_launches": int(launches), "schedule": tune, "si": si,
                 "serving": serving}
         print(json.dumps(line), flush=True)

@@ -100,6 +100,34 @@ __device__ __forceinline__ uint32_t warp_search_count(const uint32_t *__restrict
     return cnt;
 }
 
+// Same search, writing the matches: out receives the common elements in ascending order (S
+// is sorted; each round's matches are written in lane order at their ballot rank). Returns
+// the number written (warp-uniform).
+__device__ __forceinline__ uint32_t warp_search_write(const uint32_t *__restrict__ S, uint32_t s,
+                                                      const uint32_t *__restrict__ L, uint32_t l,
+                                                      uint32_t *out, int lane) {
+    uint32_t n = 0, base = 0;
+    const uint32_t lt = (1u << lane) - 1u;
+    for (uint32_t i = 0; i < s && base < l; i += 32) {
+        uint32_t k = i + lane;
+        bool valid = k < s;
+        uint32_t x = valid ? __ldg(S + k) : kEmpty;
+        uint32_t lo = base, hi = l;
+        while (lo < hi) {
+            uint32_t mid = (lo + hi) >> 1;
+            if (__ldg(L + mid) < x) lo = mid + 1;
+            else hi = mid;
+        }
+        const bool hit = valid && lo < l && __ldg(L + lo) == x;
+        const unsigned hm = __ballot_sync(kFull, hit);
+        if (hit) out[n + __popc(hm & lt)] = x;
+        n += __popc(hm);
+        uint32_t last = min(32u, s - i) - 1;
+        base = __shfl_sync(kFull, lo, last);
+    }
+    return n;
+}
+
 // Open-addressing hash of a short list in shared memory (one table per warp). The table
 // has cap = 2^lg slots with cap >= 2 * length, so every probe chain ends at an empty slot.
 __device__ __forceinline__ uint32_t hash_slot(uint32_t w, uint32_t lg) {

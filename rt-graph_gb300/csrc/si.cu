@@ -1113,6 +1113,8 @@ __global__ void __maxnreg__(96)
     }
 }
 
+constexpr uint32_t kWriteSearchRatio = 16;  // long/short above this: search, not merge
+
 __global__ void k_si_write(SiArgs s, const uint64_t *__restrict__ out_off, uint32_t *out_elems) {
     const int lane = threadIdx.x & 31;
     uint64_t warp = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5;
@@ -1122,7 +1124,14 @@ __global__ void k_si_write(SiArgs s, const uint64_t *__restrict__ out_off, uint3
         if (!pair_ids(s, k, x, y)) continue;
         uint64_t ox = s.off[x], oy = s.off[y];
         uint32_t lx = (uint32_t)(s.off[x + 1] - ox), ly = (uint32_t)(s.off[y + 1] - oy);
-        warp_merge_write(s.elems + ox, lx, s.elems + oy, ly, out_elems + out_off[k], lane);
+        // skewed pairs: the short list searched in the long one (a merge would walk the
+        // whole long list); the matches come out ascending either way
+        if ((uint64_t)ly > (uint64_t)kWriteSearchRatio * lx)
+            warp_search_write(s.elems + ox, lx, s.elems + oy, ly, out_elems + out_off[k], lane);
+        else if ((uint64_t)lx > (uint64_t)kWriteSearchRatio * ly)
+            warp_search_write(s.elems + oy, ly, s.elems + ox, lx, out_elems + out_off[k], lane);
+        else
+            warp_merge_write(s.elems + ox, lx, s.elems + oy, ly, out_elems + out_off[k], lane);
     }
 }
 

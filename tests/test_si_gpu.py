@@ -215,6 +215,25 @@ def test_materialize_matches_oracle(ctx):
     assert np.array_equal(gel, oel)
 
 
+def test_materialize_skewed_pairs_match_oracle(ctx):
+    """Lengths lognormal with sigma 2 (many pairs more than 16x apart, in both orders: the
+    write pass searches the short list in the long one) and balanced ones, against the
+    oracle's intersections, both pair orders."""
+    off, el, pa, pb, exp = rtg.gen_si_pairs(20_000, median=64.0, sigma=2.0, min_len=1,
+                                            max_len=65536, universe_log2=26, overlap_max=0.5,
+                                            seed=11)
+    lens = np.diff(off.astype(np.int64))
+    ratio = np.maximum(lens[pa], lens[pb]) / np.maximum(np.minimum(lens[pa], lens[pb]), 1)
+    assert (ratio > 16).mean() > 0.1
+    sets = ctx.sets(off, el)
+    for a, b in ((pa, pb), (pb, pa)):
+        goff, gel, _ = sets.materialize(a, b)
+        ooff, oel = oracle.si_materialize(off, el, a, b)
+        assert np.array_equal(goff, ooff)
+        assert np.array_equal(gel, oel)
+    assert np.array_equal(np.diff(goff.astype(np.int64)), exp.astype(np.int64))
+
+
 def test_vertex_pair_queries_on_graph(ctx):
     tc = tc_golden()
     s, d = golden_edges(tc["rmat_s12_ef16_s1"])
