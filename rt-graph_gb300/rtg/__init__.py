@@ -272,6 +272,23 @@ def edges_write_bin(path: str, s: np.ndarray, d: np.ndarray) -> None:
 
 
 def edges_read(path: str, fmt: int = FMT_EDGE_BIN):
+    """One read: the arrays are sized from the file (8 bytes per binary edge; a text or
+    MatrixMarket edge takes at least 3 bytes, two edges per symmetric MatrixMarket entry);
+    a file that grows between the sizing and the read falls back to the two-call form."""
+    try:
+        size = os.path.getsize(path)
+    except OSError:
+        size = -1
+    if size >= 0:
+        cap = size // 8 if fmt == FMT_EDGE_BIN else (size // 3 + 1) * (2 if fmt == FMT_MTX else 1)
+        s = np.empty(max(cap, 1), np.uint32)
+        d = np.empty(max(cap, 1), np.uint32)
+        m = C.c_uint64(cap)
+        st = lib.rtg_edges_read(str(path).encode(), fmt, C.byref(m), _ptr(s), _ptr(d))
+        if st == OK:
+            return s[: m.value].copy(), d[: m.value].copy()
+        if st != ERR_INVALID_ARG:
+            _check(st, what="edges_read")
     m = C.c_uint64(0)
     _check(lib.rtg_edges_read(str(path).encode(), fmt, C.byref(m), None, None), what="edges_read")
     s = np.empty(max(m.value, 1), np.uint32)
