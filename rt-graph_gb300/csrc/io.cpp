@@ -172,14 +172,41 @@ rtg_status read_edge_txt(const char *path, std::vector<uint32_t> &s, std::vector
     return RTG_OK;
 }
 
+// Entry lines [b, e) of a MatrixMarket body: (row, col) pairs, 1-based and checked against
+// the size line, into er/ec; empty and comment lines skipped. Stops at the first line that
+// is not an entry in range and returns its rank among the entries (er.size()), else -1.
+long long parse_mtx_entries(const char *b, const char *e, long long rows, long long cols,
+                            std::vector<uint32_t> &er, std::vector<uint32_t> &ec) {
+    while (b < e) {
+        const char *nl = static_cast<const char *>(std::memchr(b, '\n', (size_t)(e - b)));
+        const char *le = nl ? nl : e;
+        if (le != b && *b != '%') {
+            const char *p = b;
+            long long r, c;
+            if (!read_ll(p, le, r) || !read_ll(p, le, c) || r <= 0 || c <= 0 || r > rows ||
+                c > cols)
+                return (long long)er.size();
+            er.push_back((uint32_t)r);
+            ec.push_back((uint32_t)c);
+        }
+        b = nl ? nl + 1 : e;
+    }
+    return -1;
+}
+
+// Header and size line in order, then the entry lines in parallel pieces (cut after a
+// newline, one per thread); the pieces are joined in order up to nnz entries, a bad line
+// among those is a format error, lines after them are not read, and symmetric files get the
+// mirrored entry after each off-diagonal one.
 rtg_status read_mtx(const char *path, std::vector<uint32_t> &s, std::vector<uint32_t> &d) {
     std::vector<char> buf;
     if (!read_file(path, buf)) return RTG_ERR_IO;
-    enum { kHeader, kSize, kEntries, kDone } stage = kHeader;
-    bool symmetric = false, bad = false;
-    long long rows = -1, cols = -1, nnz = -1, seen = 0;
+    const char *base = buf.data(), *end = base + buf.size();
+    bool symmetric = false, bad = false, have_head = false, have_size = false;
+    long long rows = -1, cols = -1, nnz = -1;
+    const char *body = end;
     for_lines(buf, [&](const char *p, const char *e) {
-        if (stage == kHeader) {
+        if (!have_head) {
             const std::string head(p, e);
             std::string lower = head;
             for (auto &ch : lower) ch = (char)std::tolower((unsigned char)ch);
@@ -189,44 +216,67 @@ rtg_status read_mtx(const char *path, std::vector<uint32_t> &s, std::vector<uint
                 return false;
             }
             symmetric = lower.find("symmetric") != std::string::npos;
-            stage = kSize;
+            have_head = true;
             return true;
         }
         if (p == e || *p == '%') return true;  // empty and comment lines
-        if (stage == kSize) {
-            if (!read_ll(p, e, rows) || !read_ll(p, e, cols) || !read_ll(p, e, nnz)) {
-                bad = true;
-                return false;
-            }
-            if (nnz < 0) {
-                bad = true;
-                return false;
-            }
-            // every entry line takes at least 4 bytes: no reservation beyond the file
-            const size_t cap = (size_t)std::min<long long>(nnz, (long long)(buf.size() / 4 + 1));
-            s.reserve(cap * (symmetric ? 2 : 1));
-            d.reserve(cap * (symmetric ? 2 : 1));
-            stage = nnz ? kEntries : kDone;
-            return nnz != 0;
-        }
-        long long r, c;
-        if (!read_ll(p, e, r) || !read_ll(p, e, c) || r <= 0 || c <= 0 || r > rows || c > cols) {
+        if (!read_ll(p, e, rows) || !read_ll(p, e, cols) || !read_ll(p, e, nnz) || nnz < 0) {
             bad = true;
             return false;
         }
-        s.push_back((uint32_t)(r - 1));
-        d.push_back((uint32_t)(c - 1));
-        if (symmetric && r != c) {
-            s.push_back((uint32_t)(c - 1));
-            d.push_back((uint32_t)(r - 1));
-        }
-        if (++seen == nnz) {
-            stage = kDone;
-            return false;
-        }
-        return true;
+        have_size = true;
+        body = e < end ? e + 1 : end;
+        return false;
     });
-    if (bad || stage == kHeader || stage == kSize || seen != nnz) return RTG_ERR_FORMAT;
+    if (bad || !have_size) return RTG_ERR_FORMAT;
+    const size_t n = (size_t)(end - body);
+    const int T = nnz ? (int)std::max<size_t>(1, std::min<size_t>((size_t)omp_get_max_threads(),
+                                                                  n / (1u << 20) + 1))
+                      : 0;
+    std::vector<size_t> cut(T + 1, n);
+    if (T) cut[0] = 0;
+    for (int t = 1; t < T; ++t) {
+        const size_t at = std::max(cut[t - 1], n / T * t);
+        const char *nl = at < n ? static_cast<const char *>(std::memchr(body + at, '\n', n - at))
+                                : nullptr;
+        cut[t] = nl ? (size_t)(nl - body) + 1 : n;
+    }
+    std::vector<std::vector<uint32_t>> pr(T), pc(T);
+    std::vector<long long> stop(T, -1);
+#pragma omp parallel for num_threads(T > 0 ? T : 1) schedule(static, 1)
+    for (int t = 0; t < T; ++t) {
+        const size_t len = cut[t + 1] - cut[t];
+        pr[t].reserve(len / 4 + 1);
+        pc[t].reserve(len / 4 + 1);
+        stop[t] = parse_mtx_entries(body + cut[t], body + cut[t + 1], rows, cols, pr[t], pc[t]);
+    }
+    // the first nnz entries in file order; a bad line before them is a format error
+    long long seen = 0;
+    std::vector<std::pair<int, size_t>> take;  // (piece, entries taken from it)
+    for (int t = 0; t < T && seen < nnz; ++t) {
+        const long long k = std::min<long long>((long long)pr[t].size(), nnz - seen);
+        take.push_back({t, (size_t)k});
+        seen += k;
+        if (stop[t] >= 0 && seen < nnz) return RTG_ERR_FORMAT;
+    }
+    if (seen != nnz) return RTG_ERR_FORMAT;
+    size_t edges = 0;
+    for (auto &tk : take)
+        for (size_t i = 0; i < tk.second; ++i)
+            edges += (symmetric && pr[tk.first][i] != pc[tk.first][i]) ? 2 : 1;
+    s.resize(edges);
+    d.resize(edges);
+    size_t at = 0;
+    for (auto &tk : take)
+        for (size_t i = 0; i < tk.second; ++i) {
+            const uint32_t r = pr[tk.first][i], c = pc[tk.first][i];
+            s[at] = r - 1;
+            d[at++] = c - 1;
+            if (symmetric && r != c) {
+                s[at] = c - 1;
+                d[at++] = r - 1;
+            }
+        }
     return RTG_OK;
 }
 

@@ -339,3 +339,37 @@ def test_large_text_file_parses_in_parallel_pieces(tmp_path):
     gs, gd = rtg.edges_read(str(path), rtg.FMT_EDGE_TXT)
     assert np.array_equal(gs, s[keep].astype(np.uint32))
     assert np.array_equal(gd, d[keep].astype(np.uint32))
+
+
+def test_large_mtx_file_in_parallel_pieces(tmp_path):
+    """A symmetric MatrixMarket file of several MB (entry lines cut into per-thread pieces):
+    comments anywhere, mirrored off-diagonal entries in file order, a malformed line after
+    the nnz entries ignored, one before the last of them a format error."""
+    import numpy as np
+    rng = np.random.default_rng(8)
+    n, nnz = 5000, 400_000
+    r = rng.integers(1, n + 1, nnz)
+    c = rng.integers(1, n + 1, nnz)
+    rows = []
+    for i, (a, b) in enumerate(zip(r, c)):
+        if i % 101 == 0:
+            rows.append("% a comment")
+        rows.append(f"{a} {b}")
+    head = f"%%MatrixMarket matrix coordinate pattern symmetric\n{n} {n} {nnz}\n"
+    want_s, want_d = [], []
+    for a, b in zip(r, c):
+        want_s.append(a - 1)
+        want_d.append(b - 1)
+        if a != b:
+            want_s.append(b - 1)
+            want_d.append(a - 1)
+    path = tmp_path / "big.mtx"
+    path.write_text(head + "\n".join(rows) + "\nnot an entry\n1 1\n")
+    gs, gd = rtg.edges_read(str(path), rtg.FMT_MTX)
+    assert np.array_equal(gs, np.array(want_s, np.uint32))
+    assert np.array_equal(gd, np.array(want_d, np.uint32))
+    rows[-2] = "1 x"  # the next-to-last entry line malformed: fewer than nnz entries
+    path.write_text(head + "\n".join(rows) + "\n")
+    with pytest.raises(rtg.RtgError) as e:
+        rtg.edges_read(str(path), rtg.FMT_MTX)
+    assert e.value.status == rtg.ERR_FORMAT
