@@ -4,21 +4,29 @@
 // Graph::offsets_/adjs_ (tc/graph/graph.cpp:71-102), widened to 64-bit offsets.
 //
 // File (little endian):
-//   char magic[8] = "RTGCSR01"; u32 version = 1; u32 parts (bit 0 oriented, 1 counting,
+//   char magic[8] = "RTGCSR01"; u32 version = 2; u32 parts (bit 0 oriented, 1 counting,
 //   2 symmetric); u64 m_input; i32 orient; u32 zero;
 //   oriented : u32 n, u32 max_deg, u64 m, u64 work_elems, u32 has_src, u32 zero,
 //              u64 off[n+1], u32 adj[m], (u32 src[m])
 //   counting : u32 n, u32 max_deg, u64 m, u64 off[n+1], u32 adj[m], u64 in_off[n+1],
 //              uint2 in_rng[m]
 //   symmetric: u32 n, u32 max_deg, u64 m, u64 work_elems, u64 off[n+1], u32 adj[m]
-//   u64 fnv1a-64 of every byte after the magic.
+//   u64 checksum of every byte between the magic and the checksum (the payload): FNV-1a-64
+//   over the 64-bit words of each 1 MiB block (a block's last bytes one at a time), the
+//   blocks' values chained in order by FNV-1a-64 seeded with the payload length, so that
+//   the blocks are summed in parallel.
 // A file is accepted only if its checksum matches and every array describes a valid CSR
 // (offsets non-decreasing from 0 to m, ids below n, suffix ranges inside their rows), so a
-// damaged or foreign file fails with RTG_ERR_FORMAT before anything reaches a kernel.
+// damaged or foreign file fails with RTG_ERR_FORMAT before anything reaches a kernel. The
+// file is read whole and its checks run in parallel (R-MAT-21, 686 MB: 4.1 s with a
+// byte-serial checksum and serial checks before).
+#include <algorithm>
 #include <cstdio>
 #include <cstring>
 #include <string>
 #include <vector>
+
+#include <omp.h>
 
 #include "internal.h"
 
@@ -26,33 +34,53 @@ namespace rtg {
 namespace {
 
 constexpr char kMagic[8] = {'R', 'T', 'G', 'C', 'S', 'R', '0', '1'};
-constexpr uint32_t kVersion = 1;
+constexpr uint32_t kVersion = 2;
+constexpr size_t kSumBlock = size_t(1) << 20;
+
+uint64_t block_sum(const unsigned char *p, size_t n) {
+    uint64_t h = 1469598103934665603ull;
+    size_t i = 0;
+    for (; i + 8 <= n; i += 8) {
+        uint64_t w;
+        std::memcpy(&w, p + i, 8);
+        h = (h ^ w) * 1099511628211ull;
+    }
+    for (; i < n; ++i) h = (h ^ p[i]) * 1099511628211ull;
+    return h;
+}
+
+uint64_t payload_sum(const unsigned char *p, size_t n) {
+    const size_t nb = (n + kSumBlock - 1) / kSumBlock;
+    std::vector<uint64_t> bs(nb);
+#pragma omp parallel for schedule(static)
+    for (long long b = 0; b < (long long)nb; ++b)
+        bs[b] = block_sum(p + b * kSumBlock, std::min(kSumBlock, n - (size_t)b * kSumBlock));
+    uint64_t h = (1469598103934665603ull ^ (uint64_t)n) * 1099511628211ull;
+    for (uint64_t v : bs) h = (h ^ v) * 1099511628211ull;
+    return h;
+}
 constexpr uint32_t kPartOri = 1, kPartCnt = 2, kPartSym = 4;
 
+// The payload in memory; the file is written in one go with its checksum.
 struct Writer {
-    FILE *f;
-    uint64_t h = 1469598103934665603ull;
-    bool ok = true;
+    std::vector<unsigned char> buf;
     void put(const void *p, size_t bytes) {
-        if (!ok || bytes == 0) return;
         const unsigned char *c = static_cast<const unsigned char *>(p);
-        for (size_t i = 0; i < bytes; ++i) h = (h ^ c[i]) * 1099511628211ull;
-        ok = std::fwrite(p, 1, bytes, f) == bytes;
+        buf.insert(buf.end(), c, c + bytes);
     }
     template <class T> void val(T v) { put(&v, sizeof v); }
 };
 
+// The payload of a file read whole.
 struct Reader {
-    FILE *f;
-    uint64_t h = 1469598103934665603ull;
+    const unsigned char *p;
     uint64_t left;
     bool ok = true;
-    bool get(void *p, size_t bytes) {
+    bool get(void *dst, size_t bytes) {
         if (!ok || bytes > left) return ok = false;
-        if (bytes && std::fread(p, 1, bytes, f) != bytes) return ok = false;
+        if (bytes) std::memcpy(dst, p, bytes);
+        p += bytes;
         left -= bytes;
-        const unsigned char *c = static_cast<const unsigned char *>(p);
-        for (size_t i = 0; i < bytes; ++i) h = (h ^ c[i]) * 1099511628211ull;
         return true;
     }
     template <class T> bool val(T &v) { return get(&v, sizeof v); }
@@ -68,15 +96,17 @@ rtg_status to_host(rtg_ctx *ctx, const T *d, uint64_t count, std::vector<T> &h) 
 // offsets non-decreasing from 0 to m
 bool valid_offsets(const std::vector<uint64_t> &off, uint64_t n, uint64_t m) {
     if (off[0] != 0 || off[n] != m) return false;
-    for (uint64_t v = 0; v < n; ++v)
-        if (off[v + 1] < off[v]) return false;
-    return true;
+    int bad = 0;
+#pragma omp parallel for reduction(| : bad) schedule(static)
+    for (long long v = 0; v < (long long)n; ++v) bad |= off[v + 1] < off[v];
+    return !bad;
 }
 
 bool valid_ids(const std::vector<uint32_t> &ids, uint64_t m, uint64_t n) {
-    for (uint64_t i = 0; i < m; ++i)
-        if (ids[i] >= n) return false;
-    return true;
+    int bad = 0;
+#pragma omp parallel for reduction(| : bad) schedule(static)
+    for (long long i = 0; i < (long long)m; ++i) bad |= ids[i] >= n;
+    return !bad;
 }
 
 template <class T>
@@ -98,13 +128,7 @@ extern "C" rtg_status rtg_graph_save(rtg_ctx *ctx, const rtg_graph *g, const cha
                            (g->sym.built ? kPartSym : 0);
     if (!parts) return fail(ctx, RTG_ERR_STATE, "graph holds no CSR to save");
     RTG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
-    FILE *f = std::fopen(path, "wb");
-    if (!f) return fail(ctx, RTG_ERR_IO, "cannot open %s for writing", path);
-    if (std::fwrite(kMagic, 1, 8, f) != 8) {
-        std::fclose(f);
-        return fail(ctx, RTG_ERR_IO, "write failed: %s", path);
-    }
-    Writer w{f};
+    Writer w;
     w.val(kVersion);
     w.val(parts);
     w.val(g->m_input);
@@ -148,15 +172,19 @@ extern "C" rtg_status rtg_graph_save(rtg_ctx *ctx, const rtg_graph *g, const cha
             w.put(rng.data(), c.m * 8);
     }
     if (st == RTG_OK && (parts & kPartSym)) csr(g->sym, false);
-    const uint64_t h = w.h;
-    if (st == RTG_OK) w.put(&h, 8);
-    const bool ok = w.ok;
-    if (std::fclose(f) != 0 || !ok) {
+    if (st != RTG_OK) return st;
+    const uint64_t h = payload_sum(w.buf.data(), w.buf.size());
+    FILE *f = std::fopen(path, "wb");
+    if (!f) return fail(ctx, RTG_ERR_IO, "cannot open %s for writing", path);
+    bool ok = std::fwrite(kMagic, 1, 8, f) == 8 &&
+              std::fwrite(w.buf.data(), 1, w.buf.size(), f) == w.buf.size() &&
+              std::fwrite(&h, 1, 8, f) == 8;
+    if (std::fclose(f) != 0) ok = false;
+    if (!ok) {
         std::remove(path);
-        return st != RTG_OK ? st : fail(ctx, RTG_ERR_IO, "write failed: %s", path);
+        return fail(ctx, RTG_ERR_IO, "write failed: %s", path);
     }
-    if (st != RTG_OK) std::remove(path);
-    return st;
+    return RTG_OK;
 }
 
 namespace rtg {
@@ -190,28 +218,42 @@ rtg_status read_cache_file(const char *path, CacheFile &cf, std::string &why,
         why = "cannot open file";
         return RTG_ERR_IO;
     }
-    std::fseek(f, 0, SEEK_END);
-    const long long size = std::ftell(f);
-    std::fseek(f, 0, SEEK_SET);
-    char magic[8] = {};
-    if (size < 8 + 8 || std::fread(magic, 1, 8, f) != 8 || std::memcmp(magic, kMagic, 8)) {
+    std::vector<unsigned char> file;
+    {
+        long long size = -1;
+        if (std::fseek(f, 0, SEEK_END) == 0) {
+            size = std::ftell(f);
+            std::fseek(f, 0, SEEK_SET);
+        }
+        if (size > 0) file.resize((size_t)size);
+        const size_t got = size > 0 ? std::fread(file.data(), 1, (size_t)size, f) : 0;
+        const bool err = std::ferror(f) || (size > 0 && got != (size_t)size);
         std::fclose(f);
-        why = "not a CSR cache file";
-        return RTG_ERR_FORMAT;
+        if (err) {
+            why = "cannot read file";
+            return RTG_ERR_IO;
+        }
     }
-    Reader r{f, 1469598103934665603ull, (uint64_t)size - 8 - 8};  // checksum excluded
+    auto bad = [&](const char *w) {
+        why = w;
+        return RTG_ERR_FORMAT;
+    };
+    if (file.size() < 8 + 8 || std::memcmp(file.data(), kMagic, 8))
+        return bad("not a CSR cache file");
+    Reader r{file.data() + 8, (uint64_t)file.size() - 8 - 8};  // checksum excluded
     uint32_t version = 0, zero = 0;
     r.val(version);
     r.val(cf.parts);
     r.val(cf.m_input);
     r.val(cf.orient);
     r.val(zero);
-    auto bad = [&](const char *w) {
-        std::fclose(f);
-        why = w;
-        return RTG_ERR_FORMAT;
-    };
     if (!r.ok || version != kVersion || !cf.parts || (cf.parts & ~7u)) return bad("bad header");
+    {
+        uint64_t want = 0;
+        std::memcpy(&want, file.data() + file.size() - 8, 8);
+        if (payload_sum(file.data() + 8, file.size() - 16) != want)
+            return bad("checksum mismatch");
+    }
     auto read_csr = [&](HostCsr &c, bool with_src, bool with_work) -> bool {
         if (!r.val(c.n) || !r.val(c.max_deg) || !r.val(c.m)) return false;
         if (with_work && !r.val(c.work)) return false;
@@ -247,15 +289,22 @@ rtg_status read_cache_file(const char *path, CacheFile &cf, std::string &why,
         // of v must lie inside one row and hold only ranks above v; the in-edges of v are
         // ordered by source (a range never starts before the previous in-edge's), which the
         // dense-core split relies on (the in-edges from core rows are the last ones of v)
-        for (uint64_t v = 0; structure && v < hc.n; ++v)
+        int row_bad = 0, range_bad = 0, order_bad = 0;
+        const long long nv = structure ? (long long)hc.n : 0;
+#pragma omp parallel for reduction(| : row_bad) schedule(dynamic, 4096)
+        for (long long v = 0; v < nv; ++v)
             for (uint64_t q = hc.off[v]; q < hc.off[v + 1]; ++q)
-                if (hc.adj[q] <= v || (q > hc.off[v] && hc.adj[q] <= hc.adj[q - 1]))
-                    return bad("counting CSR row order");
-        for (uint64_t v = 0; structure && v < hc.n; ++v)
+                row_bad |= hc.adj[q] <= (uint64_t)v || (q > hc.off[v] && hc.adj[q] <= hc.adj[q - 1]);
+        if (row_bad) return bad("counting CSR row order");
+#pragma omp parallel for reduction(| : range_bad, order_bad) schedule(dynamic, 4096)
+        for (long long v = 0; v < nv; ++v)
             for (uint64_t e = hc.in_off[v]; e < hc.in_off[v + 1]; ++e) {
                 const uint2 rg = hc.rng[e];
-                if (rg.x > rg.y || rg.y > hc.m) return bad("suffix range");
-                if (e > hc.in_off[v] && rg.x < hc.rng[e - 1].x) return bad("in-edge order");
+                if (rg.x > rg.y || rg.y > hc.m) {
+                    range_bad = 1;
+                    continue;
+                }
+                if (e > hc.in_off[v] && rg.x < hc.rng[e - 1].x) order_bad = 1;
                 if (rg.x == rg.y) continue;
                 // the row u holding position x: last offset <= x
                 uint64_t lo = 0, hi = hc.n;
@@ -264,15 +313,14 @@ rtg_status read_cache_file(const char *path, CacheFile &cf, std::string &why,
                     if (hc.off[mid] <= rg.x) lo = mid;
                     else hi = mid - 1;
                 }
-                if (lo >= hc.n || rg.y > hc.off[lo + 1] || hc.adj[rg.x] <= v)
-                    return bad("suffix range");
+                if (lo >= hc.n || rg.y > hc.off[lo + 1] || hc.adj[rg.x] <= (uint64_t)v)
+                    range_bad = 1;
             }
+        if (range_bad) return bad("suffix range");
+        if (order_bad) return bad("in-edge order");
     }
     if ((cf.parts & kPartSym) && !read_csr(cf.sym, false, true)) return bad("symmetric CSR");
-    uint64_t want = 0, h = r.h;
-    if (!r.ok || r.left != 0 || std::fread(&want, 1, 8, f) != 8 || want != h)
-        return bad("checksum mismatch or trailing bytes");
-    std::fclose(f);
+    if (!r.ok || r.left != 0) return bad("trailing bytes");
     return RTG_OK;
 }
 

@@ -1,6 +1,7 @@
 """Counting forms written in the CSR cache file layout of csrc/csr_cache.cpp (header,
-counting part, FNV-1a-64 checksum of every byte after the magic), and forged variants of
-them: shared by the host-side file checks and the checked build's device-side checks."""
+counting part, checksum of the payload: FNV-1a-64 over the 64-bit words of each 1 MiB block,
+the block values chained by FNV-1a-64 seeded with the payload length), and forged variants
+of them: shared by the host-side file checks and the checked build's device-side checks."""
 from __future__ import annotations
 
 import struct
@@ -12,10 +13,26 @@ import oracle
 MAGIC = b"RTGCSR01"
 
 
-def fnv(data: bytes) -> int:
-    h = 1469598103934665603
-    for b in data:
-        h = ((h ^ b) * 1099511628211) & 0xFFFFFFFFFFFFFFFF
+MASK = 0xFFFFFFFFFFFFFFFF
+PRIME = 1099511628211
+BASIS = 1469598103934665603
+BLOCK = 1 << 20
+
+
+def _block_sum(data: bytes) -> int:
+    h = BASIS
+    k = len(data) // 8 * 8
+    for w in np.frombuffer(data[:k], "<u8").tolist():
+        h = ((h ^ w) * PRIME) & MASK
+    for b in data[k:]:
+        h = ((h ^ b) * PRIME) & MASK
+    return h
+
+
+def payload_sum(data: bytes) -> int:
+    h = ((BASIS ^ len(data)) * PRIME) & MASK
+    for i in range(0, len(data), BLOCK):
+        h = ((h ^ _block_sum(data[i:i + BLOCK])) * PRIME) & MASK
     return h
 
 
@@ -47,11 +64,11 @@ def counting_form(s: np.ndarray, d: np.ndarray):
 
 
 def cache_file(n, off, adj, in_off, rng, m_input=0) -> bytes:
-    body = struct.pack("<IIQiI", 1, 2, m_input, 0, 0)
+    body = struct.pack("<IIQiI", 2, 2, m_input, 0, 0)
     body += struct.pack("<IIQ", n, int(np.diff(off.astype(np.int64)).max(initial=0)), len(adj))
     body += off.astype("<u8").tobytes() + adj.astype("<u4").tobytes()
     body += in_off.astype("<u8").tobytes() + rng.astype("<u4").tobytes()
-    return MAGIC + body + struct.pack("<Q", fnv(body))
+    return MAGIC + body + struct.pack("<Q", payload_sum(body))
 
 
 

@@ -9,15 +9,9 @@ import pytest
 
 import oracle
 import rtg
+from cache_forms import payload_sum
 
 pytestmark = pytest.mark.gpu
-
-
-def fnv1a64(data: bytes) -> int:
-    h = 1469598103934665603
-    for b in data:
-        h = ((h ^ b) * 1099511628211) & 0xFFFFFFFFFFFFFFFF
-    return h
 
 
 def built_graph(ctx, scale=10, seed=5):
@@ -94,7 +88,7 @@ def test_forged_structure_with_valid_checksum_is_refused(ctx, tmp_path):
     pos += (cn + 1) * 8
     v = int(np.argmax(np.diff(off) > 0))  # first vertex with an out-neighbour
     struct.pack_into("<I", raw, pos + int(off[v]) * 4, 0 if v > 0 else v)  # rank <= v
-    raw[-8:] = struct.pack("<Q", fnv1a64(bytes(raw[8:-8])))
+    raw[-8:] = struct.pack("<Q", payload_sum(bytes(raw[8:-8])))
     forged = tmp_path / "forged.rtgcsr"
     forged.write_bytes(bytes(raw))
     with pytest.raises(rtg.RtgError) as e:

@@ -2,7 +2,7 @@
 rtg_graph_load(RTG_FMT_RTG_CSR) applies before anything reaches the device.
 
 A valid counting form is written here in the file layout of csrc/csr_cache.cpp (header,
-counting part, FNV-1a-64 checksum of every byte after the magic), then forged so that it
+counting part, block-chained FNV-1a-64 checksum of the payload), then forged so that it
 would lead the batched kernel out of its bitmap (an element at or below its vertex, rows out
 of order, a suffix range crossing into the next row or reaching below its head); every
 forgery, a flipped byte and a truncated file are refused with RTG_ERR_FORMAT.
