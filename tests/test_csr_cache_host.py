@@ -50,3 +50,31 @@ def test_forged_counting_forms_refused(tmp_path, form):
         assert _check(tmp_path, cache_file(*forged)) == rtg.ERR_FORMAT, name
     # the unforged form still passes
     assert _check(tmp_path, cache_file(*form)) == rtg.OK
+
+
+def test_directory_and_empty_file(tmp_path):
+    assert rtg.lib.rtg_graph_file_check(str(tmp_path).encode()) == rtg.ERR_IO
+    assert _check(tmp_path, b"") == rtg.ERR_FORMAT
+
+
+def test_file_read_in_pieces(tmp_path):
+    """A file of several read pieces (8 MiB each) and copy pieces (4 MiB each): accepted
+    whole, refused with one byte flipped in its last piece or one forged range in its last
+    in-edges."""
+    s, d = rtg.gen_rmat(17, 16, seed=11)
+    big = counting_form(s, d)
+    good = cache_file(*big)
+    assert len(good) > 2 * (8 << 20)
+    assert _check(tmp_path, good) == rtg.OK
+    flipped = bytearray(good)
+    flipped[len(good) - 100] ^= 4
+    assert _check(tmp_path, bytes(flipped)) == rtg.ERR_FORMAT
+    n, off, adj, in_off, rng = big
+    r = rng.copy()
+    k = len(r) - 1
+    while r[k, 0] == r[k, 1]:
+        k -= 1
+    r[k, 1] = min(int(r[k, 1]) + 1, len(adj))
+    if int(r[k, 1]) <= int(rng[k, 1]):
+        r[k, 0] = r[k, 1] + 1
+    assert _check(tmp_path, cache_file(n, off, adj, in_off, r)) == rtg.ERR_FORMAT
