@@ -43,7 +43,7 @@ extern "C" {
 typedef enum rtg_status {
     RTG_OK = 0,
     RTG_ERR_INVALID_ARG = 1, /* null pointer, size out of range, unsorted list ... */
-    RTG_ERR_OOM = 2,         /* device or pinned-host allocation failed            */
+    RTG_ERR_OOM = 2,         /* device, pinned-host or host allocation failed      */
     RTG_ERR_IO = 3,          /* file could not be opened / read / written          */
     RTG_ERR_FORMAT = 4,      /* malformed input file                               */
     RTG_ERR_DEVICE = 5,      /* CUDA runtime error (text in rtg_last_error)        */

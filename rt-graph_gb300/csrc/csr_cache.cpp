@@ -156,8 +156,17 @@ rtg_status upload(rtg_ctx *ctx, T **d, const HostVec<T> &h, uint64_t count, size
 
 using namespace rtg;
 
+static rtg_status graph_save_body(rtg_ctx *ctx, const rtg_graph *g, const char *path);
+
 extern "C" rtg_status rtg_graph_save(rtg_ctx *ctx, const rtg_graph *g, const char *path) {
     if (!ctx || !g || !path) return RTG_ERR_INVALID_ARG;
+    // the payload is assembled in host memory before the file is opened
+    const rtg_status st = host_alloc_guard([&] { return graph_save_body(ctx, g, path); });
+    if (st == RTG_ERR_OOM) return fail(ctx, st, "no host memory for the file of %s", path);
+    return st;
+}
+
+static rtg_status graph_save_body(rtg_ctx *ctx, const rtg_graph *g, const char *path) {
     const uint32_t parts = (g->ori.built ? kPartOri : 0) | (g->cnt.built ? kPartCnt : 0) |
                            (g->sym.built ? kPartSym : 0);
     if (!parts) return fail(ctx, RTG_ERR_STATE, "graph holds no CSR to save");
@@ -375,8 +384,9 @@ rtg_status read_cache_file(const char *path, CacheFile &cf, std::string &why,
 // Read a file written by rtg_graph_save into a new graph of ctx (no raw edges).
 rtg_status graph_load_cached(rtg_ctx *ctx, const char *path, rtg_graph **out) {
     CacheFile cf;
-    std::string why;
-    const rtg_status rs = read_cache_file(path, cf, why, !(kChecked && g_skip_file_structure_checks));
+    std::string why = "no host memory for the file";
+    const rtg_status rs = host_alloc_guard(
+        [&] { return read_cache_file(path, cf, why, !(kChecked && g_skip_file_structure_checks)); });
     if (rs != RTG_OK) return fail(ctx, rs, "%s: %s", path, why.c_str());
     const uint32_t parts = cf.parts;
     const uint64_t m_input = cf.m_input;
@@ -428,5 +438,5 @@ extern "C" rtg_status rtg_graph_file_check(const char *path) {
     if (!path) return RTG_ERR_INVALID_ARG;
     rtg::CacheFile cf;
     std::string why;
-    return rtg::read_cache_file(path, cf, why);
+    return rtg::host_alloc_guard([&] { return rtg::read_cache_file(path, cf, why); });
 }

@@ -10,6 +10,7 @@
 #include <string>
 #include <vector>
 
+#include "host_guard.h"
 #include "rtg.h"
 
 namespace rtg {

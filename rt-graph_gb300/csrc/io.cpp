@@ -13,6 +13,7 @@
 
 #include <omp.h>
 
+#include "host_guard.h"
 #include "rtg.h"
 
 namespace {
@@ -152,9 +153,14 @@ rtg_status read_edge_txt(const char *path, std::vector<uint32_t> &s, std::vector
 #pragma omp parallel for num_threads(T) schedule(static, 1)
     for (int t = 0; t < T; ++t) {
         const size_t len = cut[t + 1] - cut[t];
-        ps[t].reserve(len / 4 + 1);
-        pd[t].reserve(len / 4 + 1);
-        st[t] = parse_txt_lines(base + cut[t], base + cut[t + 1], ps[t], pd[t]);
+        // a failed allocation inside the parallel region stays in its piece
+        try {
+            ps[t].reserve(len / 4 + 1);
+            pd[t].reserve(len / 4 + 1);
+            st[t] = parse_txt_lines(base + cut[t], base + cut[t + 1], ps[t], pd[t]);
+        } catch (...) {
+            st[t] = RTG_ERR_OOM;
+        }
     }
     size_t total = 0;
     for (int t = 0; t < T; ++t) {
@@ -243,13 +249,21 @@ rtg_status read_mtx(const char *path, std::vector<uint32_t> &s, std::vector<uint
     }
     std::vector<std::vector<uint32_t>> pr(T), pc(T);
     std::vector<long long> stop(T, -1);
+    std::vector<char> oom(T, 0);
 #pragma omp parallel for num_threads(T > 0 ? T : 1) schedule(static, 1)
     for (int t = 0; t < T; ++t) {
         const size_t len = cut[t + 1] - cut[t];
-        pr[t].reserve(len / 4 + 1);
-        pc[t].reserve(len / 4 + 1);
-        stop[t] = parse_mtx_entries(body + cut[t], body + cut[t + 1], rows, cols, pr[t], pc[t]);
+        // a failed allocation inside the parallel region stays in its piece
+        try {
+            pr[t].reserve(len / 4 + 1);
+            pc[t].reserve(len / 4 + 1);
+            stop[t] = parse_mtx_entries(body + cut[t], body + cut[t + 1], rows, cols, pr[t], pc[t]);
+        } catch (...) {
+            oom[t] = 1;
+        }
     }
+    for (int t = 0; t < T; ++t)
+        if (oom[t]) return RTG_ERR_OOM;
     // the first nnz entries in file order; a bad line before them is a format error
     long long seen = 0;
     std::vector<std::pair<int, size_t>> take;  // (piece, entries taken from it)
@@ -284,7 +298,7 @@ rtg_status read_mtx(const char *path, std::vector<uint32_t> &s, std::vector<uint
 
 extern "C" {
 
-rtg_status rtg_edges_read(const char *path, rtg_format fmt, uint64_t *m, uint32_t *src,
+static rtg_status rtg_edges_read_body(const char *path, rtg_format fmt, uint64_t *m, uint32_t *src,
                           uint32_t *dst) {
     if (!path || !m) return RTG_ERR_INVALID_ARG;
     std::vector<uint32_t> s, d;
@@ -307,13 +321,18 @@ rtg_status rtg_edges_read(const char *path, rtg_format fmt, uint64_t *m, uint32_
     return RTG_OK;
 }
 
+rtg_status rtg_edges_read(const char *path, rtg_format fmt, uint64_t *m, uint32_t *src,
+                          uint32_t *dst) {
+    return rtg::host_alloc_guard([&] { return rtg_edges_read_body(path, fmt, m, src, dst); });
+}
+
 extern "C++" {
 namespace rtg {
 rtg_status graph_load_cached(rtg_ctx *ctx, const char *path, rtg_graph **out);  // csr_cache.cpp
 }
 }
 
-rtg_status rtg_graph_load(rtg_ctx *ctx, const char *path, rtg_format fmt, rtg_graph **out) {
+static rtg_status rtg_graph_load_body(rtg_ctx *ctx, const char *path, rtg_format fmt, rtg_graph **out) {
     if (!ctx || !path || !out) return RTG_ERR_INVALID_ARG;
     if (fmt == RTG_FMT_RTG_CSR) return rtg::graph_load_cached(ctx, path, out);
     uint64_t m = 0;
@@ -327,13 +346,18 @@ rtg_status rtg_graph_load(rtg_ctx *ctx, const char *path, rtg_format fmt, rtg_gr
     return st;
 }
 
-rtg_status rtg_edges_write_bin(const char *path, const uint32_t *src, const uint32_t *dst,
+rtg_status rtg_graph_load(rtg_ctx *ctx, const char *path, rtg_format fmt, rtg_graph **out) {
+    return rtg::host_alloc_guard([&] { return rtg_graph_load_body(ctx, path, fmt, out); });
+}
+
+static rtg_status rtg_edges_write_bin_body(const char *path, const uint32_t *src, const uint32_t *dst,
                                uint64_t m) {
     if (!path || (m && (!src || !dst))) return RTG_ERR_INVALID_ARG;
+    const uint64_t chunk = 1 << 20;
+    std::vector<int32_t> buf;
+    buf.reserve(2 * std::min<uint64_t>(m, chunk));  // before the file is opened
     FILE *f = std::fopen(path, "wb");
     if (!f) return RTG_ERR_IO;
-    std::vector<int32_t> buf;
-    const uint64_t chunk = 1 << 20;
     for (uint64_t i = 0; i < m; i += chunk) {
         uint64_t n = (m - i < chunk) ? m - i : chunk;
         buf.resize(2 * n);
@@ -353,7 +377,12 @@ rtg_status rtg_edges_write_bin(const char *path, const uint32_t *src, const uint
     return std::fclose(f) == 0 ? RTG_OK : RTG_ERR_IO;
 }
 
-rtg_status rtg_dataset_read(const char *path, rtg_dataset_info *info, uint32_t *offsets,
+rtg_status rtg_edges_write_bin(const char *path, const uint32_t *src, const uint32_t *dst,
+                               uint64_t m) {
+    return rtg::host_alloc_guard([&] { return rtg_edges_write_bin_body(path, src, dst, m); });
+}
+
+static rtg_status rtg_dataset_read_body(const char *path, rtg_dataset_info *info, uint32_t *offsets,
                             uint32_t *elems) {
     if (!path || !info) return RTG_ERR_INVALID_ARG;
     FILE *f = std::fopen(path, "rb");
@@ -364,6 +393,17 @@ rtg_status rtg_dataset_read(const char *path, rtg_dataset_info *info, uint32_t *
         return RTG_ERR_FORMAT;
     }
     const uint64_t nsets = (uint64_t)hdr[0] + hdr[1];
+    // the offsets must fit the file before they are allocated
+    long long size = -1;
+    if (std::fseek(f, 0, SEEK_END) == 0) size = std::ftell(f);
+    if (size < 0 || std::fseek(f, 16, SEEK_SET) != 0) {
+        std::fclose(f);
+        return RTG_ERR_IO;
+    }
+    if ((uint64_t)size < 16 + (nsets + 1) * 4) {
+        std::fclose(f);
+        return RTG_ERR_FORMAT;
+    }
     std::vector<uint32_t> off(nsets + 1);
     if (std::fread(off.data(), 4, nsets + 1, f) != nsets + 1) {
         std::fclose(f);
@@ -387,6 +427,11 @@ rtg_status rtg_dataset_read(const char *path, rtg_dataset_info *info, uint32_t *
     size_t got = info->elems ? std::fread(elems, 4, info->elems, f) : 0;
     std::fclose(f);
     return got == info->elems ? RTG_OK : RTG_ERR_FORMAT;
+}
+
+rtg_status rtg_dataset_read(const char *path, rtg_dataset_info *info, uint32_t *offsets,
+                            uint32_t *elems) {
+    return rtg::host_alloc_guard([&] { return rtg_dataset_read_body(path, info, offsets, elems); });
 }
 
 rtg_status rtg_dataset_write(const char *path, const rtg_dataset_info *info,

@@ -136,6 +136,25 @@ def test_bad_files_are_reported(tmp_path):
     assert e.value.status == rtg.ERR_FORMAT
 
 
+def test_dataset_header_beyond_the_file(tmp_path):
+    """A header that claims more sets than the file holds is refused before the offsets are
+    allocated (2^33 sets would take 34 GB), and a header alone is a format error too."""
+    for hdr in ([0xFFFFFFFF, 0xFFFFFFFF, 10, 0], [1 << 30, 0, 10, 0], [3, 2, 10, 0]):
+        p = tmp_path / "big.s_data"
+        p.write_bytes(np.array(hdr + [0, 1, 2], np.uint32).tobytes())
+        with pytest.raises(rtg.RtgError) as e:
+            rtg.dataset_read(str(p))
+        assert e.value.status == rtg.ERR_FORMAT, hdr
+    p.write_bytes(np.array([1, 1, 10, 0], np.uint32).tobytes())
+    with pytest.raises(rtg.RtgError) as e:
+        rtg.dataset_read(str(p))
+    assert e.value.status == rtg.ERR_FORMAT
+    # exactly the offsets and no elements: two empty sets
+    p.write_bytes(np.array([1, 1, 10, 0, 0, 0, 0], np.uint32).tobytes())
+    info, off, el = rtg.dataset_read(str(p))
+    assert (info.num_a, info.num_b, info.elems) == (1, 1, 0) and list(off) == [0, 0, 0]
+
+
 def test_dataset_roundtrip(tmp_path):
     info = rtg.DatasetInfo(2, 1, 100, 1, 5)
     off = np.array([0, 2, 4, 5], np.uint32)

@@ -373,3 +373,58 @@ def test_large_mtx_file_in_parallel_pieces(tmp_path):
     with pytest.raises(rtg.RtgError) as e:
         rtg.edges_read(str(path), rtg.FMT_MTX)
     assert e.value.status == rtg.ERR_FORMAT
+
+
+_LIMITED_CHILD = r"""
+import ctypes as C, os, resource, sys
+import rtg
+path, fmt, share = sys.argv[1], int(sys.argv[2]), float(sys.argv[3])
+vm = [int(l.split()[1]) for l in open('/proc/self/status') if l.startswith('VmSize:')][0] * 1024
+# share 1: room for the file itself, not for the parsed edges beside it; share 0.5: not
+# even for the file
+room = int(os.path.getsize(path) * share) + (24 << 20 if share >= 1 else 0)
+resource.setrlimit(resource.RLIMIT_AS, (vm + room, vm + room))
+m = C.c_uint64(0)
+if fmt < 0:
+    print(rtg.lib.rtg_graph_file_check(path.encode()))
+else:
+    print(rtg.lib.rtg_edges_read(path.encode(), fmt, C.byref(m), None, None))
+"""
+
+
+def test_host_allocation_failure_is_a_status(tmp_path):
+    """A reader or the cache check that runs out of host memory returns RTG_ERR_OOM (the
+    child limits its own address space to the file plus a little), rather than ending the
+    process with an exception through the C boundary."""
+    import os
+    import subprocess
+    import sys
+
+    import numpy as np
+
+    rng = np.random.default_rng(2)
+    e = rng.integers(0, 1 << 20, size=(3_000_000, 2))
+    txt = tmp_path / "big.txt"
+    np.savetxt(txt, e, fmt="%d")
+    env = dict(os.environ, OMP_NUM_THREADS="1")
+    pkg = os.path.dirname(os.path.dirname(rtg.__file__))
+    env["PYTHONPATH"] = pkg + os.pathsep + env.get("PYTHONPATH", "")
+
+    def limited(path, fmt, share):
+        r = subprocess.run([sys.executable, "-c", _LIMITED_CHILD, str(path), str(fmt), str(share)],
+                           env=env, capture_output=True, text=True, timeout=300)
+        assert r.returncode == 0, r.stderr[-2000:]
+        return int(r.stdout.split()[-1])
+
+    # the parse pieces fail (inside the parallel region), then the file buffer itself
+    assert limited(txt, rtg.FMT_EDGE_TXT, 1.0) == rtg.ERR_OOM
+    assert limited(txt, rtg.FMT_EDGE_TXT, 0.5) == rtg.ERR_OOM
+    # a cache file larger than the room left
+    from cache_forms import cache_file, counting_form
+    s, d = rtg.gen_rmat(17, 16, seed=3)
+    cf = tmp_path / "g.rtgcsr"
+    cf.write_bytes(cache_file(*counting_form(s, d)))
+    assert rtg.lib.rtg_graph_file_check(str(cf).encode()) == rtg.OK
+    assert limited(cf, -1, 0.5) == rtg.ERR_OOM
+    # the same file without the limit reads
+    assert len(rtg.edges_read(str(txt), rtg.FMT_EDGE_TXT)[0]) == len(e)
