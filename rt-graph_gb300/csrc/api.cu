@@ -177,6 +177,9 @@ void rtg_destroy(rtg_ctx *ctx) {
     dev_free(ctx->d_scalars);
     for (auto &ev : ctx->ev)
         if (ev) cudaEventDestroy(ev);
+    for (auto &ev : ctx->stage_ev)
+        if (ev) cudaEventDestroy(ev);
+    if (ctx->h_stage) cudaFreeHost(ctx->h_stage);
     cudaStreamDestroy(ctx->stream);
     delete ctx;
 }
@@ -1077,6 +1080,65 @@ rtg_status rtg_si_count_dense(rtg_ctx *ctx, const rtg_sets *s, uint32_t a_begin,
     return si_run(ctx, ps, nullptr, nullptr, out_counts, flags & ~RTG_PAIRS_DEVICE, timing);
 }
 
+// Device-to-host copy of `bytes` into caller memory, enqueued on the context stream (the
+// caller synchronises). Page-locked destinations and small copies go straight there. A
+// large pageable destination is filled through two page-locked staging buffers: each
+// chunk's copy over the host link runs while the host threads move the previous chunk into
+// the caller's pages (the driver's own pageable path maps and fills those pages on one
+// thread). Without staging memory the copy goes straight there too.
+constexpr size_t kStageBytes = size_t(32) << 20;
+
+static rtg_status d2h_copy(rtg_ctx *ctx, void *dst, const void *src, size_t bytes) {
+    if (!bytes) return RTG_OK;
+    if (bytes >= 2 * kStageBytes && !mapped_host(dst) && !ctx->h_stage) {
+        void *h = nullptr;
+        cudaEvent_t e[2] = {};
+        bool ok = cudaHostAlloc(&h, 2 * kStageBytes, cudaHostAllocDefault) == cudaSuccess;
+        for (auto &x : e) ok = ok && cudaEventCreateWithFlags(&x, cudaEventDisableTiming) == cudaSuccess;
+        if (ok) {
+            ctx->h_stage = h;
+            ctx->stage_ev[0] = e[0];
+            ctx->stage_ev[1] = e[1];
+        } else {  // no staging: the copy goes straight to the caller's memory
+            cudaGetLastError();
+            for (auto &x : e)
+                if (x) cudaEventDestroy(x);
+            if (h) cudaFreeHost(h);
+        }
+    }
+    if (bytes < 2 * kStageBytes || !ctx->h_stage || mapped_host(dst)) {
+        RTG_CUDA(ctx, cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, ctx->stream));
+        return RTG_OK;
+    }
+    char *stage = static_cast<char *>(ctx->h_stage);
+    const size_t chunks = (bytes + kStageBytes - 1) / kStageBytes;
+    // chunk i lands in stage half i % 2; that half's previous chunk (i - 2) was moved out in
+    // the iteration before
+    for (size_t i = 0; i <= chunks; ++i) {
+        if (i < chunks) {
+            const size_t len = std::min(kStageBytes, bytes - i * kStageBytes);
+            RTG_CUDA(ctx, cudaMemcpyAsync(stage + (i & 1) * kStageBytes,
+                                          static_cast<const char *>(src) + i * kStageBytes, len,
+                                          cudaMemcpyDeviceToHost, ctx->stream));
+            RTG_CUDA(ctx, cudaEventRecord(ctx->stage_ev[i & 1], ctx->stream));
+        }
+        if (i > 0) {
+            const size_t j = i - 1, len = std::min(kStageBytes, bytes - j * kStageBytes);
+            RTG_CUDA(ctx, cudaEventSynchronize(ctx->stage_ev[j & 1]));
+            char *to = static_cast<char *>(dst) + j * kStageBytes;
+            const char *from = stage + (j & 1) * kStageBytes;
+            constexpr size_t kPiece = size_t(1) << 20;
+            const long long pieces = (long long)((len + kPiece - 1) / kPiece);
+#pragma omp parallel for schedule(static)
+            for (long long q = 0; q < pieces; ++q) {
+                const size_t a = (size_t)q * kPiece;
+                std::memcpy(to + a, from + a, std::min(kPiece, len - a));
+            }
+        }
+    }
+    return RTG_OK;
+}
+
 // Count -> scan -> write for the pairs of ps, then the offsets and elements to the host.
 static rtg_status materialize_to_host(rtg_ctx *ctx, const PairSpec &ps, uint64_t *out_offsets,
                                       uint32_t *out_elems, uint64_t out_capacity,
@@ -1098,11 +1160,8 @@ static rtg_status materialize_to_host(rtg_ctx *ctx, const PairSpec &ps, uint64_t
                                           &ctx->launches);
     if (st != RTG_OK && st != RTG_ERR_INVALID_ARG) return st;
     RTG_CUDA(ctx, cudaEventRecord(ctx->ev[1], ctx->stream));
-    RTG_CUDA(ctx, cudaMemcpyAsync(out_offsets, d_off, (npairs + 1) * 8, cudaMemcpyDeviceToHost,
-                                  ctx->stream));
-    if (st == RTG_OK && needed)
-        RTG_CUDA(ctx, cudaMemcpyAsync(out_elems, d_elems, needed * 4, cudaMemcpyDeviceToHost,
-                                      ctx->stream));
+    RTG_TRY(d2h_copy(ctx, out_offsets, d_off, (npairs + 1) * 8));
+    if (st == RTG_OK && needed) RTG_TRY(d2h_copy(ctx, out_elems, d_elems, needed * 4));
     RTG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
     RTG_TRY(check_status_word(ctx));
     if (st != RTG_OK)

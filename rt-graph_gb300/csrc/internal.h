@@ -105,6 +105,10 @@ struct rtg_ctx {
     uint32_t *d_status = nullptr;        // device status word (kernels write errors here)
     unsigned long long *d_scalars = nullptr;  // small device scratch for counters (16 words)
     cudaEvent_t ev[8] = {};
+    // page-locked staging for device-to-host copies into pageable caller memory (two
+    // buffers, allocated on the first such copy) and the events that mark their copies
+    void *h_stage = nullptr;
+    cudaEvent_t stage_ev[2] = {};
     // grow-only scratch for CUB temp storage and per-call buffers
     rtg::DeviceBuffer scratch[9];
     // grow-only temporaries of the CSR builder (kept between builds: no allocation, and
