@@ -1080,12 +1080,13 @@ rtg_status rtg_si_count_dense(rtg_ctx *ctx, const rtg_sets *s, uint32_t a_begin,
     return si_run(ctx, ps, nullptr, nullptr, out_counts, flags & ~RTG_PAIRS_DEVICE, timing);
 }
 
-// Device-to-host copy of `bytes` into caller memory, enqueued on the context stream (the
-// caller synchronises). Page-locked destinations and small copies go straight there. A
-// large pageable destination is filled through two page-locked staging buffers: each
-// chunk's copy over the host link runs while the host threads move the previous chunk into
-// the caller's pages (the driver's own pageable path maps and fills those pages on one
-// thread). Without staging memory the copy goes straight there too.
+// Device-to-host copy of `bytes` into caller memory after the work on the context stream.
+// Page-locked destinations and small copies go straight there, only enqueued (the caller
+// synchronises the stream). A large pageable destination is filled through two page-locked
+// staging buffers, and the call returns once it is filled: each chunk's copy over the host
+// link runs while the host threads move the previous chunk into the caller's pages (the
+// driver's own pageable path maps and fills those pages on one thread). Without staging
+// memory the copy goes straight there too.
 constexpr size_t kStageBytes = size_t(32) << 20;
 
 static rtg_status d2h_copy(rtg_ctx *ctx, void *dst, const void *src, size_t bytes) {
