@@ -78,3 +78,17 @@ def test_file_read_in_pieces(tmp_path):
     if int(r[k, 1]) <= int(rng[k, 1]):
         r[k, 0] = r[k, 1] + 1
     assert _check(tmp_path, cache_file(n, off, adj, in_off, r)) == rtg.ERR_FORMAT
+
+
+def test_other_versions_and_parts_refused(tmp_path, form):
+    """A file of another format version, with no part or an unknown part bit, is refused."""
+    import struct
+
+    from cache_forms import MAGIC, payload_sum
+    good = cache_file(*form)
+    body = bytearray(good[8:-8])
+    for version, parts in ((1, 2), (3, 2), (2, 0), (2, 8 | 2)):
+        b = bytearray(body)
+        b[0:8] = struct.pack("<II", version, parts)
+        data = MAGIC + bytes(b) + struct.pack("<Q", payload_sum(bytes(b)))
+        assert _check(tmp_path, data) == rtg.ERR_FORMAT, (version, parts)
