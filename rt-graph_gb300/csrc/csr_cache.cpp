@@ -135,7 +135,7 @@ struct Writer {
 // Write n bytes at p to a new file at path, in pieces by the host threads; on any failure
 // the partial file is removed.
 bool write_file(const char *path, const unsigned char *p, size_t n) {
-    const int fd = ::open(path, O_WRONLY | O_CREAT | O_TRUNC, 0644);
+    const int fd = ::open(path, O_WRONLY | O_CREAT | O_TRUNC | O_CLOEXEC, 0644);
     if (fd < 0) return false;
     constexpr size_t kPiece = size_t(8) << 20;
     const long long pieces = (long long)((n + kPiece - 1) / kPiece);
@@ -293,7 +293,7 @@ struct CacheFile {
 // checks of that build.
 rtg_status read_cache_file(const char *path, CacheFile &cf, std::string &why,
                            bool structure = true) {
-    const int fd = ::open(path, O_RDONLY);
+    const int fd = ::open(path, O_RDONLY | O_CLOEXEC);
     if (fd < 0) {
         why = "cannot open file";
         return RTG_ERR_IO;
