@@ -1086,12 +1086,14 @@ rtg_status rtg_si_count_dense(rtg_ctx *ctx, const rtg_sets *s, uint32_t a_begin,
 // staging buffers, and the call returns once it is filled: each chunk's copy over the host
 // link runs while the host threads move the previous chunk into the caller's pages (the
 // driver's own pageable path maps and fills those pages on one thread). Without staging
-// memory the copy goes straight there too.
-constexpr size_t kStageBytes = size_t(32) << 20;
+// memory the copy goes straight there too. Chunks are an eighth of the copy, 4 to 32 MB,
+// so that a copy of a few tens of MB still overlaps its pieces.
+constexpr size_t kStageBytes = size_t(32) << 20;  // each of the two staging buffers
+constexpr size_t kStageMin = size_t(16) << 20;    // smaller copies go straight there
 
 static rtg_status d2h_copy(rtg_ctx *ctx, void *dst, const void *src, size_t bytes) {
     if (!bytes) return RTG_OK;
-    if (bytes >= 2 * kStageBytes && !mapped_host(dst) && !ctx->h_stage) {
+    if (bytes >= kStageMin && !mapped_host(dst) && !ctx->h_stage) {
         void *h = nullptr;
         cudaEvent_t e[2] = {};
         bool ok = cudaHostAlloc(&h, 2 * kStageBytes, cudaHostAllocDefault) == cudaSuccess;
@@ -1107,26 +1109,28 @@ static rtg_status d2h_copy(rtg_ctx *ctx, void *dst, const void *src, size_t byte
             if (h) cudaFreeHost(h);
         }
     }
-    if (bytes < 2 * kStageBytes || !ctx->h_stage || mapped_host(dst)) {
+    if (bytes < kStageMin || !ctx->h_stage || mapped_host(dst)) {
         RTG_CUDA(ctx, cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, ctx->stream));
         return RTG_OK;
     }
     char *stage = static_cast<char *>(ctx->h_stage);
-    const size_t chunks = (bytes + kStageBytes - 1) / kStageBytes;
+    const size_t C = std::min(kStageBytes,
+                              std::max(size_t(4) << 20, (bytes / 8 + 4095) & ~size_t(4095)));
+    const size_t chunks = (bytes + C - 1) / C;
     // chunk i lands in stage half i % 2; that half's previous chunk (i - 2) was moved out in
     // the iteration before
     for (size_t i = 0; i <= chunks; ++i) {
         if (i < chunks) {
-            const size_t len = std::min(kStageBytes, bytes - i * kStageBytes);
+            const size_t len = std::min(C, bytes - i * C);
             RTG_CUDA(ctx, cudaMemcpyAsync(stage + (i & 1) * kStageBytes,
-                                          static_cast<const char *>(src) + i * kStageBytes, len,
+                                          static_cast<const char *>(src) + i * C, len,
                                           cudaMemcpyDeviceToHost, ctx->stream));
             RTG_CUDA(ctx, cudaEventRecord(ctx->stage_ev[i & 1], ctx->stream));
         }
         if (i > 0) {
-            const size_t j = i - 1, len = std::min(kStageBytes, bytes - j * kStageBytes);
+            const size_t j = i - 1, len = std::min(C, bytes - j * C);
             RTG_CUDA(ctx, cudaEventSynchronize(ctx->stage_ev[j & 1]));
-            char *to = static_cast<char *>(dst) + j * kStageBytes;
+            char *to = static_cast<char *>(dst) + j * C;
             const char *from = stage + (j & 1) * kStageBytes;
             constexpr size_t kPiece = size_t(1) << 20;
             const long long pieces = (long long)((len + kPiece - 1) / kPiece);

@@ -217,17 +217,18 @@ def test_triangle_lists_match_oracle(ctx, name):
     assert len(np.unique((np.sort(np.stack([u, v, x]), axis=0) * [[1 << 42], [1 << 21], [1]]).sum(0))) == len(w)
 
 
-def test_triangle_lists_large_staged(ctx):
+@pytest.mark.parametrize("scale", [16, 18])
+def test_triangle_lists_large_staged(ctx, scale):
     """Lists large enough that their copy to pageable host memory goes through the
-    page-locked staging buffers (several 32 MB chunks, the last one partial): bit-exact
-    against the oracle's per-pair merge."""
-    s, d = rtg.gen_rmat(18, 16, 0.57, 0.19, 0.19, seed=5)
+    page-locked staging buffers (R-MAT 16: 60 MB in chunks of an eighth; R-MAT 18: 316 MB in
+    32 MB chunks, the last one partial): bit-exact against the oracle's per-pair merge."""
+    s, d = rtg.gen_rmat(scale, 16, 0.57, 0.19, 0.19, seed=5)
     g = ctx.graph_from_edges(s, d).build(rtg.ORIENT_DEGREE)
     off, adj = g.csr()
     n = len(off) - 1
     src = np.repeat(np.arange(n, dtype=np.uint32), np.diff(off.astype(np.int64)))
     loff, w, t = g.tc_list()
-    assert len(w) * 4 > 3 * (32 << 20) and (len(w) * 4) % (32 << 20) != 0
+    assert len(w) * 4 >= 16 << 20
     ooff, ow = oracle.si_materialize(off, adj, src, adj)
     assert np.array_equal(loff, ooff)
     assert np.array_equal(w, ow)
